@@ -1,0 +1,317 @@
+"""CPU oracle for the RHF + MP2 path -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may
+import this module, always as the checker.  It restates the upstream algorithm:
+
+* AO bookkeeping: atoms in input order, shells in basis-library order, spherical
+  functions in the rows of ``Data/transform_basis.py:3-12`` (``Util/structures.py:464-523``).
+* one-electron S and H = T + V via ``hgp_oracle.c`` (``Methods/integrals.py:220-370``),
+  assembled like ``Methods/hartree_fock.py:207-224``.
+* canonical orthogonalisation X = U s^{-1/2}, eigenvalues sorted descending and
+  s <= 1e-6 dropped (``Methods/hartree_fock.py:226-237``, ``Data/constants.py:34``).
+* Schwarz-screened ERIs: diagonal (ab|ab) always, other unique shell quartets when
+  max_ab * max_cd > 1e-8 (``Methods/hartree_fock.py:244-297``, ``Data/constants.py:31``).
+* RHF through the UHF machinery with identical spins: J = einsum('cd,abcd->ab'),
+  K = einsum('cb,abcd->ad') (``Methods/hartree_fock.py:329-355``), DIIS C1 on the
+  residual X^T(SDF - FDS)X (``Methods/hf_extensions/diis.py:14-139``), energy
+  0.5 sum(D_tot H + D_a F_a + D_b F_b) (``Methods/hartree_fock.py:188-201``).
+  ``mode='reference'`` keeps upstream's choices (energy from the extrapolated Fock,
+  |dE| stop only); ``mode='consistent'`` (the default judge) takes the energy from the
+  Fock built from the current density and stops on |dE| < 1e-10 and D-RMS < 1e-8.
+* MP2: closed-shell form of ``Methods/mp2.py:43-94`` (identical value for RHF).
+"""
+import ctypes
+import json
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "libhgp_oracle.so")
+BASIS_JSON = os.path.join(REPO, "pychem_gb300", "data", "basis_sets.json")
+TO_BOHR = 1.8897161646320724        # Data/constants.py:2
+INTEGRAL_THRESHOLD = 1.0e-8         # Data/constants.py:31
+LINEAR_DEPENDENCE = 1.0e-6          # Data/constants.py:34
+NELEC = {"H": 1, "HE": 2, "LI": 3, "BE": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "NE": 10}
+
+
+class OrShell(ctypes.Structure):
+    _fields_ = [("l", ctypes.c_int), ("nprim", ctypes.c_int), ("center", ctypes.c_double * 3),
+                ("exps", ctypes.c_double * 16), ("ccs", ctypes.c_double * 16)]
+
+
+def build(force=False):
+    """Compile the C oracle (gcc, no GPU)."""
+    src = os.path.join(HERE, "hgp_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-o", LIB_PATH, src, "-lm"])
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.POINTER
+        L.oracle_eri_quartet.argtypes = [P(OrShell)] * 4 + [P(ctypes.c_double)]
+        L.oracle_one_electron.argtypes = [P(OrShell), P(OrShell), ctypes.c_int, P(ctypes.c_double),
+                                          P(ctypes.c_double)] + [P(ctypes.c_double)] * 3
+        L.oracle_eri_list.argtypes = [P(OrShell), ctypes.c_int, P(ctypes.c_int)]
+        L.oracle_eri_list.restype = ctypes.c_double
+        L.oracle_boys.argtypes = [ctypes.c_int, ctypes.c_double, P(ctypes.c_double)]
+        assert L.oracle_sizeof_shell() == ctypes.sizeof(OrShell)
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def boys(mmax, T):
+    out = np.zeros(mmax + 1)
+    lib().oracle_boys(mmax, float(T), _dp(out))
+    return out
+
+
+class Basis:
+    """Shells of a molecule in upstream AO order."""
+
+    def __init__(self, atoms, basis_name):
+        """atoms: list of (symbol, Z, x, y, z) with coordinates in bohr."""
+        with open(BASIS_JSON) as fh:
+            lib_sets = json.load(fh)
+        key = basis_name.replace("*", "s").replace("-", "").replace("(", "").replace(")", "").replace(",", "").upper()
+        data = lib_sets[key]
+        self.atoms = [(a[0].upper(), float(a[1]), np.array(a[2:5], dtype=float)) for a in atoms]
+        self.shells = []      # (l, exps, ccs, centre, atom index)
+        for ia, (sym, Z, xyz) in enumerate(self.atoms):
+            for fn in data[sym]:
+                l = fn[0]
+                exps = np.array([p[0] for p in fn[1:]], dtype=float)
+                ccs = np.array([p[1] for p in fn[1:]], dtype=float)
+                self.shells.append((l, exps, ccs, xyz, ia))
+        self.offsets = []
+        n = 0
+        for s in self.shells:
+            self.offsets.append(n)
+            n += 2 * s[0] + 1
+        self.nbf = n
+        self.c = (OrShell * len(self.shells))()
+        for i, (l, exps, ccs, xyz, _) in enumerate(self.shells):
+            self.c[i].l = l
+            self.c[i].nprim = len(exps)
+            for k in range(3):
+                self.c[i].center[k] = xyz[k]
+            for k in range(len(exps)):
+                self.c[i].exps[k] = exps[k]
+                self.c[i].ccs[k] = ccs[k]
+        self.nuc_xyz = np.ascontiguousarray([a[2] for a in self.atoms], dtype=float).reshape(-1, 3)
+        self.nuc_z = np.array([a[1] for a in self.atoms], dtype=float)
+
+    @property
+    def nshell(self):
+        return len(self.shells)
+
+    def nelectrons(self, charge=0):
+        return sum(NELEC[a[0]] for a in self.atoms) - charge
+
+    def nuclear_repulsion(self):
+        e = 0.0
+        for i in range(len(self.atoms)):
+            for j in range(i):
+                r = np.linalg.norm(self.atoms[i][2] - self.atoms[j][2])
+                e += self.atoms[i][1] * self.atoms[j][1] / r
+        return e
+
+    def shell_block(self, a, b, c, d):
+        na, nb, nc, nd = (2 * self.shells[s][0] + 1 for s in (a, b, c, d))
+        out = np.zeros(na * nb * nc * nd)
+        rc = lib().oracle_eri_quartet(ctypes.byref(self.c[a]), ctypes.byref(self.c[b]),
+                                      ctypes.byref(self.c[c]), ctypes.byref(self.c[d]), _dp(out))
+        if rc != 0:
+            raise ValueError("oracle supports shells up to d")
+        return out.reshape(na, nb, nc, nd)
+
+    def one_electron(self):
+        S = np.zeros((self.nbf, self.nbf))
+        H = np.zeros((self.nbf, self.nbf))
+        for a in range(self.nshell):
+            for b in range(a, self.nshell):
+                na, nb = 2 * self.shells[a][0] + 1, 2 * self.shells[b][0] + 1
+                s = np.zeros(na * nb); t = np.zeros(na * nb); v = np.zeros(na * nb)
+                lib().oracle_one_electron(ctypes.byref(self.c[a]), ctypes.byref(self.c[b]), len(self.atoms),
+                                          _dp(self.nuc_xyz), _dp(self.nuc_z), _dp(s), _dp(t), _dp(v))
+                oa, ob = self.offsets[a], self.offsets[b]
+                S[oa:oa + na, ob:ob + nb] = s.reshape(na, nb)
+                S[ob:ob + nb, oa:oa + na] = s.reshape(na, nb).T
+                h = (t + v).reshape(na, nb)
+                H[oa:oa + na, ob:ob + nb] = h
+                H[ob:ob + nb, oa:oa + na] = h.T
+        return S, H
+
+    def schwarz(self):
+        """Per shell pair: max over functions of sqrt((mn|mn)) (hartree_fock.py:244-254)."""
+        Q = np.zeros((self.nshell, self.nshell))
+        for a in range(self.nshell):
+            for b in range(a, self.nshell):
+                blk = self.shell_block(a, b, a, b)
+                na, nb = blk.shape[:2]
+                diag = np.array([[blk[m, n, m, n] for n in range(nb)] for m in range(na)])
+                Q[a, b] = Q[b, a] = math.sqrt(max(0.0, diag.max()))
+        return Q
+
+    def quartets(self, Q=None):
+        """Canonical unique shell quartets kept by the upstream screening rule."""
+        if Q is None:
+            Q = self.schwarz()
+        pairs = [(a, b) for a in range(self.nshell) for b in range(a, self.nshell)]
+        out = []
+        for i, (a, b) in enumerate(pairs):
+            for j in range(i + 1):
+                c, d = pairs[j]
+                if i == j or Q[a, b] * Q[c, d] > INTEGRAL_THRESHOLD:
+                    out.append((a, b, c, d))
+        return out
+
+    def eri_dense(self):
+        n = self.nbf
+        eri = np.zeros((n, n, n, n))
+        for (a, b, c, d) in self.quartets():
+            blk = self.shell_block(a, b, c, d)
+            oa, ob, oc, od = (self.offsets[s] for s in (a, b, c, d))
+            sa, sb, sc, sd = blk.shape
+            A, B, C, D = slice(oa, oa + sa), slice(ob, ob + sb), slice(oc, oc + sc), slice(od, od + sd)
+            eri[A, B, C, D] = blk
+            eri[B, A, C, D] = blk.transpose(1, 0, 2, 3)
+            eri[A, B, D, C] = blk.transpose(0, 1, 3, 2)
+            eri[B, A, D, C] = blk.transpose(1, 0, 3, 2)
+            eri[C, D, A, B] = blk.transpose(2, 3, 0, 1)
+            eri[D, C, A, B] = blk.transpose(3, 2, 0, 1)
+            eri[C, D, B, A] = blk.transpose(2, 3, 1, 0)
+            eri[D, C, B, A] = blk.transpose(3, 2, 1, 0)
+        return eri
+
+
+def pack8(eri):
+    """8-fold unique packing (i>=j, k>=l, ij>=kl), pair index i(i+1)/2+j."""
+    n = eri.shape[0]
+    ii, jj = np.tril_indices(n)
+    P, Q = np.tril_indices(len(ii))
+    return eri[ii[P], jj[P], ii[Q], jj[Q]].copy()
+
+
+def unpack8(packed, n):
+    ii, jj = np.tril_indices(n)
+    npair = len(ii)
+    M = np.zeros((npair, npair))
+    P, Q = np.tril_indices(npair)
+    M[P, Q] = packed
+    M[Q, P] = packed
+    eri = np.zeros((n, n, n, n))
+    eri[ii[:, None], jj[:, None], ii[None, :], jj[None, :]] = M
+    eri[jj[:, None], ii[:, None], ii[None, :], jj[None, :]] = M
+    eri[ii[:, None], jj[:, None], jj[None, :], ii[None, :]] = M
+    eri[jj[:, None], ii[:, None], jj[None, :], ii[None, :]] = M
+    return eri
+
+
+def orthogonaliser(S):
+    s, U = np.linalg.eigh(S)
+    order = s.argsort()[::-1]
+    U = U[:, order]
+    s = s[order]
+    keep = s > LINEAR_DEPENDENCE
+    return U[:, keep] * (s[keep] ** -0.5)
+
+
+def rhf(S, H, eri, nocc, e_nuc, mode="consistent", max_iter=200, e_tol=1e-10, d_tol=1e-8,
+        diis_size=None, D0=None):
+    """Returns dict(E, C, eps, D, iterations, converged)."""
+    X = orthogonaliser(S)
+    Xt = X.T
+
+    def diag(F):
+        e, Cp = np.linalg.eigh(Xt @ F @ X)
+        return e, X @ Cp
+
+    if D0 is None:
+        eps, C = diag(H)
+        D = C[:, :nocc] @ C[:, :nocc].T
+    else:
+        D = D0.copy()
+    F = H.copy()
+
+    def fock(D):
+        J = np.einsum("cd,abcd->ab", 2.0 * D, eri, optimize=True)
+        K = np.einsum("cb,abcd->ad", D, eri, optimize=True)
+        return H + J - K
+
+    def energy(D, F):
+        return 0.5 * np.sum(2.0 * D * H) + np.sum(D * F) + e_nuc
+
+    E = energy(D, F if mode == "reference" else fock(D))
+    focks, resids = [], []
+    converged = False
+    it = 0
+    for it in range(1, max_iter + 1):
+        F = fock(D)
+        E_cons = energy(D, F)
+        R = Xt @ (S @ D @ F - F @ D @ S) @ X
+        Fx = F
+        if it > 1 and (mode == "consistent" or abs(R.max()) < 0.5):
+            focks.append(F.copy())
+            resids.append(R.copy())
+            if diis_size and len(focks) > diis_size:
+                focks.pop(0); resids.pop(0)
+            if len(focks) > 1:
+                while True:
+                    m = len(focks)
+                    B = -np.ones((m + 1, m + 1))
+                    B[m, m] = 0.0
+                    for i in range(m):
+                        for j in range(m):
+                            B[i, j] = np.sum(resids[i] * resids[j])
+                    ev = np.abs(np.linalg.eigvals(B))
+                    if ev.min() > 0 and ev.max() / ev.min() <= 1e7 or m <= 2:
+                        break
+                    focks.pop(0); resids.pop(0)
+                rhs = np.zeros(m + 1)
+                rhs[m] = -1.0
+                c = np.linalg.solve(B, rhs)[:m]
+                Fx = sum(ci * Fi for ci, Fi in zip(c, focks))
+        eps, C = diag(Fx)
+        D_new = C[:, :nocc] @ C[:, :nocc].T
+        if mode == "reference":
+            E_new = energy(D_new, Fx)
+        else:
+            E_new = energy(D_new, fock(D_new))
+        dE = E_new - E
+        drms = math.sqrt(np.mean((D_new - D) ** 2))
+        D, E = D_new, E_new
+        if mode == "reference":
+            if abs(dE) < e_tol:
+                converged = True
+                break
+        elif abs(dE) < e_tol and drms < d_tol:
+            converged = True
+            break
+    F = fock(D)
+    eps, C = diag(F)
+    return dict(E=E, C=C, eps=eps, D=D, iterations=it, converged=converged, F=F)
+
+
+def rmp2(C, eps, eri, nocc):
+    """Closed-shell MP2 correlation energy from the dense AO ERI tensor."""
+    Co, Cv = C[:, :nocc], C[:, nocc:]
+    ovov = np.einsum("pi,qa,rj,sb,pqrs->iajb", Co, Cv, Co, Cv, eri, optimize=True)
+    eo, ev = eps[:nocc], eps[nocc:]
+    denom = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
+    return float(np.sum(ovov * (2.0 * ovov - ovov.transpose(0, 3, 2, 1)) / denom))

@@ -1,0 +1,250 @@
+"""Generate the golden fixtures in this folder from the upstream pychem reference.
+
+Run once in a container that holds the reference tree (``PYCHEM_REFERENCE``,
+default ``/root/reference``):
+
+    python tests/golden/make_golden.py
+
+Outputs (all small, committed):
+
+* ``<case>.npz``      S, core H, ERIs (dense for <= 13 AO, 8-fold packed otherwise),
+                      RHF/MP2 energies of the patched reference at |dE| < 1e-11,
+                      coordinates in bohr, atom list, basis name.
+* ``c_ints_calls.npz`` + ``c_ints_calls.json``: recorded inputs and outputs of the
+                      reference ``_c_ints`` extension's 11 functions, captured while
+                      ``integrals.one_electron``/``two_electron`` ran on H2O cc-pVDZ.
+* ``ref_energies.json``: final energies printed in the reference's own test outputs
+                      (``Tests/example*.out``) and the same inputs re-run here tightly.
+"""
+import json
+import math
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import refrun  # noqa: E402
+
+OUT_FUNCS = {
+    "shellpair_quantities": (0, 1, 2),
+    "two_electron_bound": (0,),
+    "two_electron_fundamentals": (0, 7),
+    "two_electron_vrr": (0,),
+    "two_electron_contract": (0,),
+    "two_electron_hrr": (0,),
+    "one_electron_fundamentals": (0,),
+    "one_electron_vrr": (0,),
+    "one_electron_hrr": (0,),
+    "one_electron_kinetic": (0,),
+    "one_electron_contract": (0,),
+}
+
+
+def water(angle_deg=104.52, r=0.9572):
+    th = math.radians(angle_deg)
+    return [["O", 8.0, 0.0, 0.0, 0.0], ["H", 1.0, r, 0.0, 0.0],
+            ["H", 1.0, r * math.cos(th), r * math.sin(th), 0.0]]
+
+
+def jittered_dimer(seed=7):
+    """Two waters 2.9 Angstrom apart, each rotated and jittered (seeded)."""
+    rng = np.random.default_rng(seed)
+    base = np.array([a[2:] for a in water()], dtype=float)
+    atoms = []
+    for k, shift in enumerate(([0.0, 0.0, 0.0], [2.9, 0.0, 0.0])):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                      [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+        xyz = base @ R.T + np.array(shift) + rng.normal(scale=0.05, size=(3, 3))
+        for (lab, Z), p in zip((("O", 8.0), ("H", 1.0), ("H", 1.0)), xyz):
+            atoms.append([lab, Z, float(p[0]), float(p[1]), float(p[2])])
+    return atoms
+
+
+def pack8(eri):
+    """8-fold unique packing: pair ij = i(i+1)/2+j (i>=j), value at IJ(IJ+1)/2+KL (IJ>=KL)."""
+    n = eri.shape[0]
+    ii, jj = np.tril_indices(n)
+    npair = len(ii)
+    pairs = np.arange(npair)
+    P, Q = np.tril_indices(npair)
+    return eri[ii[P], jj[P], ii[Q], jj[Q]].copy()
+
+
+def run_case(ns, name, coords, basis, units="ANGSTROM", mp2=False, dense=True):
+    mol, st = refrun.molecule_from_spec(ns, coords, basis, units=units,
+                                        method="MP2" if mp2 else "HF")
+    ns["hartree_fock"].do(st, mol, st.BasisSets[0], 0)
+    state = mol.States[0]
+    out = dict(
+        basis=np.array(basis), atoms=np.array([a[0] for a in coords]),
+        charges=np.array([a[1] for a in coords], dtype=float),
+        coords_bohr=np.array([a.Coordinates for a in mol.Atoms], dtype=float),
+        S=mol.Overlap.copy(), H=mol.Core.copy(), E_nuc=np.array(mol.NuclearRepulsion),
+        E_rhf=np.array(state.TotalEnergy), mo_energies=np.array(state.Alpha.Energies),
+    )
+    if dense:
+        out["eri_dense"] = mol.CoulombIntegrals.copy()
+    else:
+        out["eri_packed"] = pack8(mol.CoulombIntegrals)
+    if mp2:
+        ecorr = ns["mp2"].do(st, mol)
+        out["E_mp2_corr"] = np.array(ecorr)
+        out["E_mp2_total"] = np.array(state.TotalEnergy + ecorr)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("%-22s N=%3d  E_rhf=%.12f%s" % (name, mol.NOrbitals, state.TotalEnergy,
+          ("  E_mp2=%.12f" % out["E_mp2_total"]) if mp2 else ""))
+    return mol, st
+
+
+class Recorder:
+    """Wraps the reference _c_ints functions and keeps a few calls per function."""
+
+    def __init__(self, modules, per_func=10):
+        self.modules = modules
+        self.per_func = per_func
+        self.calls = []
+        self.sigs = {}
+        self.orig = {fn: getattr(modules[0], fn) for fn in OUT_FUNCS}
+        for m in modules:
+            for fn in OUT_FUNCS:
+                setattr(m, fn, self._wrap(fn))
+
+    def _wrap(self, fn):
+        orig = self.orig[fn]
+
+        def wrapped(*args):
+            sig = tuple(a for a in args if isinstance(a, (int, float)) and not isinstance(a, bool))
+            seen = self.sigs.setdefault(fn, set())
+            keep = len(seen) < self.per_func and sig not in seen
+            if keep:
+                seen.add(sig)
+                before = [self._snap(a) for a in args]
+            orig(*args)
+            if keep:
+                after = [self._snap(args[i]) for i in OUT_FUNCS[fn]]
+                self.calls.append((fn, before, after))
+        return wrapped
+
+    @staticmethod
+    def _snap(a):
+        if isinstance(a, np.ndarray):
+            return np.array(a, dtype=np.float64, copy=True)
+        if isinstance(a, list):
+            return [np.array(x, dtype=np.float64, copy=True) for x in a]
+        return a
+
+    def restore(self):
+        for m in self.modules:
+            for fn in OUT_FUNCS:
+                setattr(m, fn, self.orig[fn])
+
+    def save(self, stem):
+        arrays, manifest = {}, []
+        for k, (fn, before, after) in enumerate(self.calls):
+            args = []
+            for i, a in enumerate(before):
+                if isinstance(a, np.ndarray):
+                    key = "c%d_a%d" % (k, i)
+                    arrays[key] = a
+                    args.append(["array", key])
+                elif isinstance(a, list):
+                    keys = []
+                    for j, x in enumerate(a):
+                        key = "c%d_a%d_%d" % (k, i, j)
+                        arrays[key] = x
+                        keys.append(key)
+                    args.append(["list", keys])
+                elif isinstance(a, float):
+                    args.append(["float", a])
+                else:
+                    args.append(["int", int(a)])
+            outs = []
+            for i, a in zip(OUT_FUNCS[fn], after):
+                key = "c%d_o%d" % (k, i)
+                arrays[key] = a
+                outs.append([i, key])
+            manifest.append({"fn": fn, "args": args, "outputs": outs})
+        np.savez_compressed(stem + ".npz", **arrays)
+        with open(stem + ".json", "w") as fh:
+            json.dump(manifest, fh, indent=0)
+        counts = {}
+        for m in manifest:
+            counts[m["fn"]] = counts.get(m["fn"], 0) + 1
+        print("recorded calls:", counts)
+
+
+def record_fine_grained(ns):
+    import Methods
+    modules = [ns["c_ints"], Methods._c_ints]
+    rec = Recorder(modules)
+    mol, st = refrun.molecule_from_spec(ns, water(), "cc-pVDZ")
+    sp = mol.ShellPairs
+    for key in [(0, 0), (3, 5), (5, 5), (6, 8), (2, 11), (0, 3), (4, 9)]:
+        ns["integrals"].one_electron(mol, sp[key])
+    for bra, ket in [((0, 0), (0, 0)), ((3, 3), (0, 3)), ((5, 5), (5, 5)), ((3, 5), (6, 8)),
+                     ((0, 5), (2, 4)), ((7, 11), (3, 9)), ((1, 6), (4, 5)), ((2, 2), (3, 4))]:
+        ns["integrals"].two_electron(sp[bra], sp[ket], 0, -1.0)
+    # two_electron_bound is only reached from commented-out code upstream; exercise it directly
+    rng = np.random.default_rng(3)
+    for dims in [(1, 1, 1, 1), (3, 1, 3, 3), (5, 3, 1, 5)]:
+        nla, nlb, nlc, nld = dims
+        bounds = np.zeros(nla * nlb * nlc * nld)
+        C_P = rng.uniform(0.0, 2.0, size=(nla, nlb))
+        C_Q = rng.uniform(0.0, 2.0, size=(nlc, nld))
+        getattr(modules[0], "two_electron_bound")(bounds, C_P, C_Q, nla, nlb, nlc, nld)
+    rec.restore()
+    rec.save(os.path.join(HERE, "c_ints_calls"))
+
+
+EXAMPLE_OUTS = {
+    # file, section coordinates (bohr), basis, printed final HF energy line
+    "example5": ("H2", [["H", 1.0, 0.0, 0.0, 0.0], ["H", 1.0, 1.398397232, 0.0, 0.0]], "STO-3G", "BOHR"),
+    "example6": ("LiH", [["Li", 3.0, 0.0, 0.0, 0.0], ["H", 1.0, 3.013923978561, 0.0, 0.0]], "STO-3G", "BOHR"),
+    "example7": ("BH", [["B", 5.0, 0.0, 0.0, 0.0], ["H", 1.0, 3.013923978561, 0.0, 0.0]], "STO-3G", "BOHR"),
+    "example4": ("H2", [["H", 1.0, 0.0, 0.0, 0.0], ["H", 1.0, 1.0, 0.0, 0.0]], "6-311G", "ANGSTROM"),
+}
+
+
+def final_energy_from_out(path):
+    text = open(path).read()
+    vals = re.findall(r"Final HF energy:\s*([-0-9.eE+]+)", text)
+    if vals:
+        return float(vals[-1])
+    vals = re.findall(r"[Tt]otal energy:?\s*([-0-9.eE+]+)", text)
+    return float(vals[-1]) if vals else None
+
+
+def reference_examples(ns):
+    res = {}
+    for ex, (label, coords, basis, units) in EXAMPLE_OUTS.items():
+        printed = final_energy_from_out(os.path.join(refrun.REFERENCE, "Tests", ex + ".out"))
+        mol, st = refrun.molecule_from_spec(ns, coords, basis, units=units)
+        ns["hartree_fock"].do(st, mol, st.BasisSets[0], 0)
+        res[ex] = {"molecule": label, "basis": basis, "units": units, "coords": coords,
+                   "printed_final_energy": printed,
+                   "tight_energy": float(mol.States[0].TotalEnergy)}
+        print(ex, label, basis, printed, res[ex]["tight_energy"])
+    with open(os.path.join(HERE, "ref_energies.json"), "w") as fh:
+        json.dump(res, fh, indent=1)
+
+
+def main():
+    root = refrun.prepare()
+    ns = refrun.load(root)
+    run_case(ns, "h2o_sto3g", water(), "STO-3G", mp2=True)
+    run_case(ns, "h2o_631g", water(), "6-31G", mp2=True)
+    run_case(ns, "h2o_ccpvdz", water(), "cc-pVDZ", dense=False)
+    run_case(ns, "water_dimer_631g", jittered_dimer(), "6-31G", dense=False)
+    reference_examples(ns)
+    record_fine_grained(ns)
+
+
+if __name__ == "__main__":
+    main()
