@@ -1,0 +1,185 @@
+/*
+ * pychem_gb300 -- C ABI of the GB300 (sm_103a) Hartree-Fock integral and SCF library.
+ *
+ * Two layers, both plain C (pointers, sizes, an opaque CUDA stream handle):
+ *
+ *  1. Drop-in layer for the upstream `_c_ints` CPython extension
+ *     (Methods/_c_ints.c:68-81).  One function per upstream method, same argument
+ *     order and meaning; arrays are HOST buffers laid out exactly as the upstream
+ *     NumPy arrays (C-contiguous float64), outputs are written in place (the contract
+ *     functions accumulate, as upstream).  Each call copies to the GPU, runs one
+ *     kernel, copies back and synchronises.  Return value: 0 on success, otherwise a
+ *     PCG_ERR_* code with a message from pcg_last_error().
+ *
+ *  2. Batched whole-molecule layer used by the GPU SCF: DEVICE pointers, caller-owned
+ *     buffers, an explicit stream, asynchronous.  Replaces the per-quartet Python loops
+ *     of Methods/hartree_fock.py:207-355 (core matrices, Schwarz pass, screened ERI
+ *     store, J/K contraction).
+ */
+#ifndef PYCHEM_GB300_H
+#define PYCHEM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCG_OK 0
+#define PCG_ERR_CUDA 1
+#define PCG_ERR_ARG 2
+#define PCG_ERR_UNSUPPORTED 3
+#define PCG_ERR_NOTINIT 4
+#define PCG_ERR_CAPACITY 5
+
+/* ---------------------------------------------------------------------------------
+ * Library
+ * --------------------------------------------------------------------------------- */
+int pcg_version(void);
+const char *pcg_last_error(void);
+/* Build the Boys-function table on the current device (idempotent). */
+int pcg_device_init(void);
+
+/* ---------------------------------------------------------------------------------
+ * 1. Drop-in layer: the 11 methods of the upstream `_c_ints` module.
+ *    Shapes below use ncart(l) = (l+1)(l+2)/2; "[r][c]" means r*c doubles row-major.
+ * --------------------------------------------------------------------------------- */
+
+/* Methods/_c_ints.c:114-154 (c_ints/shellpair_quantities.c:5-38).
+ * sigmas, overlaps [n_alpha][n_beta]; centres [n_alpha][n_beta][3]. */
+int pcg_shellpair_quantities(double *sigmas, double *overlaps, double *centres,
+                             const double *alpha_exps, const double *A, int n_alpha,
+                             const double *beta_exps, const double *B, int n_beta);
+
+/* Methods/_c_ints.c:158-191 (c_ints/two_electron_bound.c:5-27).
+ * bounds [nla*nlb*nlc*nld]; C_P [nla][nlb]; C_Q [nlc][nld]. */
+int pcg_two_electron_bound(double *bounds, const double *C_P, const double *C_Q,
+                           int nla, int nlb, int nlc, int nld);
+
+/* Methods/_c_ints.c:195-245 (c_ints/two_electron_fundamentals.c:6-95).
+ * fundamentals [m+1][na*nb][nc*nd]; sigma/U [na][nb], [nc][nd]; P [na][nb][3];
+ * Q [nc][nd][3]; R [na*nb][nc*nd][3] (output).  ints_type 1 (scattering) is not
+ * part of this library and returns PCG_ERR_UNSUPPORTED. */
+int pcg_two_electron_fundamentals(double *fundamentals, const double *sigma_P, const double *U_P,
+                                  const double *P, const double *sigma_Q, const double *U_Q,
+                                  const double *Q, double *R, int na, int nb, int nc, int nd,
+                                  int m, int ints_type, double grid_value);
+
+/* Methods/_c_ints.c:249-301 (c_ints/two_electron_vrr.c:4-141).
+ * target [ncart(lbra)*na*nb][ncart(lket)*nc*nd]; base0/base1 [ncart(lbra-1)*na*nb][..];
+ * base2/base3 [ncart(lbra-2)*na*nb][..] (read when lbra >= 2); base4
+ * [ncart(lbra-1)*na*nb][ncart(lket-1)*nc*nd] (read when lket >= 1); zeta [na][nb];
+ * eta [nc][nd]; kappa [na] (kappa_index 0) or [nb]; Rx [3]; R [na*nb][nc*nd][3]. */
+int pcg_two_electron_vrr(double *target, const double *base0, const double *base1,
+                         const double *base2, const double *base3, const double *base4,
+                         const double *zeta, const double *eta, const double *kappa,
+                         const double *Rx, const double *R, int na, int nb, int nc, int nd,
+                         int lbra, int lket, int kappa_index);
+
+/* Methods/_c_ints.c:305-344 (c_ints/two_electron_contract.c:3-57); accumulates.
+ * contracted [ncart(lbra)][ncart(lket)]; primitive [ncart(lbra)*na*nb][ncart(lket)*nc*nd]. */
+int pcg_two_electron_contract(double *contracted, const double *primitive, const double *cc_bra,
+                              const double *cc_ket, int na, int nb, int nc, int nd, int lbra,
+                              int lket);
+
+/* Methods/_c_ints.c:348-385 (c_ints/two_electron_hrr.c:4-94).
+ * goofy 0: target [ncart(la)*ncart(lb+1)][ncart(lc)*ncart(ld)], base0 (la+1, lb),
+ * base1 (la, lb); goofy 1: target [ncart(la+1)*ncart(lb)][..], base0 (la, lb+1),
+ * base1 (la, lb), rows of base0 indexed with the upstream stride. */
+int pcg_two_electron_hrr(double *target, const double *base0, const double *base1,
+                         const double *Rx, int la, int lb, int lc, int ld, int goofy);
+
+/* Methods/_c_ints.c:389-431 (c_ints/one_electron_fundamentals.c:6-103).
+ * fundamentals [m+1][na][nb]; Rc [3]. */
+int pcg_one_electron_fundamentals(double *fundamentals, const double *sigma_P, const double *U_P,
+                                  const double *P, const double *Rc, double Z, int na, int nb,
+                                  int m);
+
+/* Methods/_c_ints.c:435-501 (c_ints/one_electron_vrr.c:4-82); base_list holds n_base
+ * pointers.  atom_index -1: overlap (base0 [ncart(la-1)*na][nb], base1
+ * [ncart(la-2)*na][nb]); otherwise nuclear attraction (base0, base1 [ncart(la-1)*na][nb],
+ * base2, base3 [ncart(la-2)*na][nb]).  target [ncart(la)*na][nb]. */
+int pcg_one_electron_vrr(double *target, const double *const *base_list, const double *sigma_P,
+                         const double *P, const double *Ra, const double *Rc, int atom_index,
+                         int n_base, int na, int nb, int la);
+
+/* Methods/_c_ints.c:505-552 (c_ints/one_electron_hrr.c:4-75).
+ * target [ncart(la)*na][ncart(lb)*nb]; base0 (la+1, lb-1); base1 (la, lb-1). */
+int pcg_one_electron_hrr(double *target, const double *const *base_list, const double *Rab,
+                         int n_base, int na, int nb, int la, int lb);
+
+/* Methods/_c_ints.c:556-605 (c_ints/one_electron_kinetic.c:4-75).
+ * target [ncart(la)*na][ncart(lb)*nb]; base0 (la, lb+2), base1 (la, lb), base2 (la, lb-2). */
+int pcg_one_electron_kinetic(double *target, const double *const *base_list, const double *exB,
+                             int n_base, int na, int nb, int la, int lb);
+
+/* Methods/_c_ints.c:609-644 (c_ints/one_electron_contract.c:3-51); accumulates.
+ * target [ncart(la)][ncart(lb)]; base [ncart(la)*na][ncart(lb)*nb]; cc [na][nb]. */
+int pcg_one_electron_contract(double *target, const double *base, const double *cc, int na,
+                              int nb, int la, int lb);
+
+/* ---------------------------------------------------------------------------------
+ * 2. Batched layer (device pointers, asynchronous on `stream`, a cudaStream_t).
+ * --------------------------------------------------------------------------------- */
+
+/* Shells of a molecule in upstream AO order (Util/structures.py:464-523).
+ * pr_cc: contraction coefficient times (2a)^{(l+1.5)/2} times the normalisation of
+ * the pure-axis Cartesian component (Util/structures.py:843,850-856). */
+typedef struct {
+  int nshell, nprim, natom, nbf;
+  const int *sh_l, *sh_nprim, *sh_prim, *sh_ao, *sh_atom;
+  const double *sh_xyz, *pr_exp, *pr_cc, *at_xyz, *at_z;
+} pcg_basis_t;
+
+/* Shell pairs (A = higher angular momentum) and their primitive-pair data. */
+typedef struct {
+  int npair, npp;
+  const int *A, *B, *ppoff, *npp_of;
+  const double *AB, *zeta, *P, *PA, *K, *oo2z;
+  const float *Kf;
+} pcg_pairs_t;
+
+/* Primitive-pair data for npair pairs (replaces the per-pair ShellPair set-up,
+ * Util/structures.py:918-956).  Outputs sized npair*3 (AB) and npp (*3). */
+int pcg_pair_data(const pcg_basis_t *basis, int npair, const int *A, const int *B,
+                  const int *ppoff, double *AB, double *zeta, double *P, double *PA, double *K,
+                  float *Kf, double *oo2z, void *stream);
+
+/* Overlap S and core Hamiltonian H = T + V, nbf x nbf, all shell pairs listed
+ * (Methods/hartree_fock.py:207-224 over Methods/integrals.py:220-370). */
+int pcg_one_electron(const pcg_basis_t *basis, int npair, const int *A, const int *B, double *S,
+                     double *H, void *stream);
+
+/* ERI class id of (la lb|lc ld), la>=lb, lc>=ld, pair class of bra >= ket; -1 if none. */
+int pcg_eri_class_id(int la, int lb, int lc, int ld);
+/* spherical elements per quartet of a class */
+int pcg_eri_class_nout(int cls);
+
+/* Contracted, normalised spherical blocks of ntask quartets (tasks = ntask int pairs
+ * {bra pair, ket pair}) of one class into store[k*ntask + t].  fp32 != 0 computes in
+ * single precision (for quartets below the mixed-precision Schwarz threshold). */
+int pcg_eri_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
+                  int ntask, double *store, int fp32, void *stream);
+
+/* Schwarz factor Q[pair] = sqrt(max (mn|mn)) from diagonal blocks of a diagonal class. */
+int pcg_schwarz_class(int cls, const int *tasks, int ntask, const double *store, double *Q,
+                      void *stream);
+
+/* Expand one bucket of screened quartets into task pairs (see eri.cu k_expand). */
+int pcg_expand_tasks(int nbra, const int *bra, const int *ket, const long long *off,
+                     const int *qstart, const int *diag, long long ntask, int *out_tasks,
+                     void *stream);
+
+/* Closed-shell Fock digestion: G += contributions of the stored blocks of one class
+ * with density D (nbf x nbf); F = H + (G + G^T)/2 via pcg_fock_build. */
+int pcg_digest_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
+                     int ntask, const double *store, const double *D, double *G, void *stream);
+int pcg_fock_build(int n, const double *H, const double *G, double *F, void *stream);
+
+/* Scatter the stored blocks of one class into a dense nbf^4 tensor with the 8-fold
+ * symmetry (Methods/hartree_fock.py:314-325). */
+int pcg_dense_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
+                    int ntask, const double *store, double *eri, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

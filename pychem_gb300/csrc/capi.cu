@@ -1,0 +1,114 @@
+// C ABI of the batched layer (include/pychem_gb300.h, section 2) and error handling.
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/pychem_gb300.h"
+#include "common.cuh"
+#include "pcg_internal.h"
+
+static thread_local char g_err[512] = "";
+
+void pcg_set_error(const char* msg) { snprintf(g_err, sizeof(g_err), "%s", msg); }
+void pcg_set_cuda_error(cudaError_t e, const char* what) {
+  snprintf(g_err, sizeof(g_err), "CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+}
+
+int pcg_launch_schwarz(int cls, const int2* tasks, int ntask, const double* store, double* Q, cudaStream_t s);
+int pcg_launch_expand(int nbra, const int* bra, const int* ket, const long long* off, const int* qstart,
+                      const int* diag, long long ntask, int2* out, cudaStream_t s);
+int pcg_launch_fock(int n, const double* H, const double* G, double* F, cudaStream_t s);
+
+static DevBasis to_dev(const pcg_basis_t* b) {
+  DevBasis d;
+  d.nshell = b->nshell; d.nprim = b->nprim; d.natom = b->natom; d.nbf = b->nbf;
+  d.sh_l = b->sh_l; d.sh_nprim = b->sh_nprim; d.sh_prim = b->sh_prim; d.sh_ao = b->sh_ao;
+  d.sh_atom = b->sh_atom; d.sh_xyz = b->sh_xyz; d.pr_exp = b->pr_exp; d.pr_cc = b->pr_cc;
+  d.at_xyz = b->at_xyz; d.at_z = b->at_z;
+  return d;
+}
+
+static DevPairsExt to_dev(const pcg_pairs_t* p) {
+  DevPairsExt d;
+  d.p.npair = p->npair; d.p.npp = p->npp;
+  d.p.A = p->A; d.p.B = p->B; d.p.ppoff = p->ppoff; d.p.npp_of = p->npp_of;
+  d.p.AB = p->AB; d.p.zeta = p->zeta; d.p.P = p->P; d.p.PA = p->PA; d.p.K = p->K; d.p.Kf = p->Kf;
+  d.oo2z = p->oo2z;
+  return d;
+}
+
+extern "C" {
+
+int pcg_version(void) { return 1; }
+
+const char* pcg_last_error(void) { return g_err; }
+
+int pcg_device_init(void) {
+  BoysTable bt;
+  return pcg_ensure_boys(&bt);
+}
+
+int pcg_pair_data(const pcg_basis_t* basis, int npair, const int* A, const int* B, const int* ppoff,
+                  double* AB, double* zeta, double* P, double* PA, double* K, float* Kf, double* oo2z,
+                  void* stream) {
+  if (!basis || npair < 0) { pcg_set_error("pcg_pair_data: bad arguments"); return PCG_ERR_ARG; }
+  return pcg_launch_pair_data(to_dev(basis), npair, A, B, ppoff, AB, zeta, P, PA, K, Kf, oo2z,
+                              (cudaStream_t)stream);
+}
+
+int pcg_one_electron(const pcg_basis_t* basis, int npair, const int* A, const int* B, double* S, double* H,
+                     void* stream) {
+  if (!basis || npair < 0) { pcg_set_error("pcg_one_electron: bad arguments"); return PCG_ERR_ARG; }
+  BoysTable bt;
+  int rc = pcg_ensure_boys(&bt);
+  if (rc) return rc;
+  return pcg_launch_one_electron(to_dev(basis), bt, npair, A, B, S, H, (cudaStream_t)stream);
+}
+
+int pcg_eri_class_id(int la, int lb, int lc, int ld) { return pcg_class_id(la, lb, lc, ld); }
+
+int pcg_eri_class_nout(int cls) { return pcg_class_nout(cls); }
+
+int pcg_eri_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                  double* store, int fp32, void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs || ntask < 0) {
+    pcg_set_error("pcg_eri_class: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  BoysTable bt;
+  int rc = pcg_ensure_boys(&bt);
+  if (rc) return rc;
+  return pcg_launch_eri(cls, to_dev(basis), to_dev(pairs), bt, (const int2*)tasks, ntask, store, fp32 ? 1 : 0,
+                        0.0f, nullptr, (cudaStream_t)stream);
+}
+
+int pcg_schwarz_class(int cls, const int* tasks, int ntask, const double* store, double* Q, void* stream) {
+  int rc = pcg_launch_schwarz(cls, (const int2*)tasks, ntask, store, Q, (cudaStream_t)stream);
+  if (rc == PCG_ERR_ARG) pcg_set_error("pcg_schwarz_class: not a diagonal class");
+  return rc;
+}
+
+int pcg_expand_tasks(int nbra, const int* bra, const int* ket, const long long* off, const int* qstart,
+                     const int* diag, long long ntask, int* out_tasks, void* stream) {
+  if (nbra <= 0 && ntask > 0) { pcg_set_error("pcg_expand_tasks: no bra pairs"); return PCG_ERR_ARG; }
+  return pcg_launch_expand(nbra, bra, ket, off, qstart, diag, ntask, (int2*)out_tasks, (cudaStream_t)stream);
+}
+
+int pcg_digest_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                     const double* store, const double* D, double* G, void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs) { pcg_set_error("pcg_digest_class: bad arguments"); return PCG_ERR_ARG; }
+  return pcg_launch_digest(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, D, G,
+                           (cudaStream_t)stream);
+}
+
+int pcg_fock_build(int n, const double* H, const double* G, double* F, void* stream) {
+  return pcg_launch_fock(n, H, G, F, (cudaStream_t)stream);
+}
+
+int pcg_dense_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                    const double* store, double* eri, void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs) { pcg_set_error("pcg_dense_class: bad arguments"); return PCG_ERR_ARG; }
+  return pcg_launch_dense(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, eri,
+                          (cudaStream_t)stream);
+}
+
+}  // extern "C"

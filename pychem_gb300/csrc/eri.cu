@@ -1,0 +1,293 @@
+// Electron-repulsion integrals over Schwarz-screened shell quartets, Fock digestion
+// and dense expansion.
+//
+// Upstream counterparts: Methods/integrals.py:427-555 (two_electron: fundamentals,
+// VRR, contraction, HRR, normalisation, spherical transform),
+// Methods/c_ints/two_electron_{fundamentals,vrr,contract,hrr}.c, the screened quartet
+// loop and 8-fold store of Methods/hartree_fock.py:241-325, and the J/K contraction
+// of Methods/hartree_fock.py:329-355.
+//
+// Layout: one task = one canonical shell quartet (bra pair, ket pair) of a class;
+// tasks of a class are grouped in buckets of equal primitive counts so a warp runs
+// uniform loops.  Results of a class are stored class-major
+//     store[k * ntask + t]   (k = spherical element, t = task)
+// so writes here and reads in the digestion are coalesced across a warp.
+#include "common.cuh"
+#include "pcg_internal.h"
+
+// ----------------------------------------------------------------------------------
+// Fock digestion (closed shell): for every stored quartet block, with the shell-level
+// degeneracy d = (A!=B ? 2:1)(C!=D ? 2:1)(AB!=CD ? 2:1) and v' = d (ab|cd),
+//   G_ab += D_cd v', G_cd += D_ab v', G_ac -= D_bd v'/4, G_bd -= D_ac v'/4,
+//   G_ad -= D_bc v'/4, G_bc -= D_ad v'/4;
+// the caller symmetrises F = H + (G + G^T)/2, which equals H + 2J[D] - K[D] with D the
+// alpha density -- upstream's H + J[D_a + D_b] - K[D_a] (hartree_fock.py:345-355).
+// ----------------------------------------------------------------------------------
+template <int NA, int NB, int NC, int ND>
+__global__ void __launch_bounds__(128) k_digest(DevBasis b, DevPairsExt pr, const int2* __restrict__ tasks,
+                                                int ntask, const double* __restrict__ store,
+                                                const double* __restrict__ D, double* __restrict__ G) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  const int2 tk = tasks[t];
+  const int A = __ldg(pr.p.A + tk.x), B = __ldg(pr.p.B + tk.x);
+  const int C = __ldg(pr.p.A + tk.y), Dd = __ldg(pr.p.B + tk.y);
+  const int oa = __ldg(b.sh_ao + A), ob = __ldg(b.sh_ao + B), oc = __ldg(b.sh_ao + C), od = __ldg(b.sh_ao + Dd);
+  const int n = b.nbf;
+  const double deg = (A == B ? 1.0 : 2.0) * (C == Dd ? 1.0 : 2.0) * (tk.x == tk.y ? 1.0 : 2.0);
+  double Dab[NA][NB], Dcd[NC][ND], Dac[NA][NC], Dbd[NB][ND], Dad[NA][ND], Dbc[NB][NC];
+  double gab[NA][NB], gcd[NC][ND], gac[NA][NC], gbd[NB][ND], gad[NA][ND], gbc[NB][NC];
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) { Dab[i][j] = __ldg(D + (size_t)(oa + i) * n + ob + j); gab[i][j] = 0.0; }
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int l = 0; l < ND; ++l) { Dcd[k][l] = __ldg(D + (size_t)(oc + k) * n + od + l); gcd[k][l] = 0.0; }
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { Dac[i][k] = __ldg(D + (size_t)(oa + i) * n + oc + k); gac[i][k] = 0.0; }
+#pragma unroll
+  for (int j = 0; j < NB; ++j)
+#pragma unroll
+    for (int l = 0; l < ND; ++l) { Dbd[j][l] = __ldg(D + (size_t)(ob + j) * n + od + l); gbd[j][l] = 0.0; }
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+#pragma unroll
+    for (int l = 0; l < ND; ++l) { Dad[i][l] = __ldg(D + (size_t)(oa + i) * n + od + l); gad[i][l] = 0.0; }
+#pragma unroll
+  for (int j = 0; j < NB; ++j)
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { Dbc[j][k] = __ldg(D + (size_t)(ob + j) * n + oc + k); gbc[j][k] = 0.0; }
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+#pragma unroll
+      for (int k = 0; k < NC; ++k)
+#pragma unroll
+        for (int l = 0; l < ND; ++l) {
+          const double v = deg * __ldg(store + (size_t)(((i * NB + j) * NC + k) * ND + l) * ntask + t);
+          const double vq = -0.25 * v;
+          gab[i][j] = fma(Dcd[k][l], v, gab[i][j]);
+          gcd[k][l] = fma(Dab[i][j], v, gcd[k][l]);
+          gac[i][k] = fma(Dbd[j][l], vq, gac[i][k]);
+          gbd[j][l] = fma(Dac[i][k], vq, gbd[j][l]);
+          gad[i][l] = fma(Dbc[j][k], vq, gad[i][l]);
+          gbc[j][k] = fma(Dad[i][l], vq, gbc[j][k]);
+        }
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) atomicAdd(G + (size_t)(oa + i) * n + ob + j, gab[i][j]);
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int l = 0; l < ND; ++l) atomicAdd(G + (size_t)(oc + k) * n + od + l, gcd[k][l]);
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+#pragma unroll
+    for (int k = 0; k < NC; ++k) atomicAdd(G + (size_t)(oa + i) * n + oc + k, gac[i][k]);
+#pragma unroll
+  for (int j = 0; j < NB; ++j)
+#pragma unroll
+    for (int l = 0; l < ND; ++l) atomicAdd(G + (size_t)(ob + j) * n + od + l, gbd[j][l]);
+#pragma unroll
+  for (int i = 0; i < NA; ++i)
+#pragma unroll
+    for (int l = 0; l < ND; ++l) atomicAdd(G + (size_t)(oa + i) * n + od + l, gad[i][l]);
+#pragma unroll
+  for (int j = 0; j < NB; ++j)
+#pragma unroll
+    for (int k = 0; k < NC; ++k) atomicAdd(G + (size_t)(ob + j) * n + oc + k, gbc[j][k]);
+}
+
+// Dense N^4 store with the 8-fold permutational symmetry (hartree_fock.py:314-325).
+template <int NA, int NB, int NC, int ND>
+__global__ void k_dense(DevBasis b, DevPairsExt pr, const int2* __restrict__ tasks, int ntask,
+                        const double* __restrict__ store, double* __restrict__ eri) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  const int2 tk = tasks[t];
+  const int oa = b.sh_ao[pr.p.A[tk.x]], ob = b.sh_ao[pr.p.B[tk.x]];
+  const int oc = b.sh_ao[pr.p.A[tk.y]], od = b.sh_ao[pr.p.B[tk.y]];
+  const size_t n = b.nbf;
+  for (int i = 0; i < NA; ++i)
+    for (int j = 0; j < NB; ++j)
+      for (int k = 0; k < NC; ++k)
+        for (int l = 0; l < ND; ++l) {
+          const double v = store[(size_t)(((i * NB + j) * NC + k) * ND + l) * ntask + t];
+          const size_t a = oa + i, bb = ob + j, c = oc + k, d = od + l;
+          eri[((a * n + bb) * n + c) * n + d] = v;
+          eri[((bb * n + a) * n + c) * n + d] = v;
+          eri[((a * n + bb) * n + d) * n + c] = v;
+          eri[((bb * n + a) * n + d) * n + c] = v;
+          eri[((c * n + d) * n + a) * n + bb] = v;
+          eri[((d * n + c) * n + a) * n + bb] = v;
+          eri[((c * n + d) * n + bb) * n + a] = v;
+          eri[((d * n + c) * n + bb) * n + a] = v;
+        }
+}
+
+// Schwarz factor per shell pair from its diagonal block (ab|ab): sqrt(max (mn|mn)),
+// the upstream bound of hartree_fock.py:244-254 reduced to the pair level.
+template <int NA, int NB>
+__global__ void k_schwarz(const int2* __restrict__ tasks, int ntask, const double* __restrict__ store,
+                          double* __restrict__ Q) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  double m = 0.0;
+  for (int i = 0; i < NA; ++i)
+    for (int j = 0; j < NB; ++j) {
+      const double v = store[(size_t)(((i * NB + j) * NA + i) * NB + j) * ntask + t];
+      m = fmax(m, v);
+    }
+  Q[tasks[t].x] = sqrt(m);
+}
+
+// ----------------------------------------------------------------------------------
+// Class table and dispatch
+// ----------------------------------------------------------------------------------
+static const int kClassL[21][4] = {
+    {0, 0, 0, 0}, {1, 0, 0, 0}, {1, 0, 1, 0}, {1, 1, 0, 0}, {1, 1, 1, 0}, {1, 1, 1, 1}, {2, 0, 0, 0},
+    {2, 0, 1, 0}, {2, 0, 1, 1}, {2, 0, 2, 0}, {2, 1, 0, 0}, {2, 1, 1, 0}, {2, 1, 1, 1}, {2, 1, 2, 0},
+    {2, 1, 2, 1}, {2, 2, 0, 0}, {2, 2, 1, 0}, {2, 2, 1, 1}, {2, 2, 2, 0}, {2, 2, 2, 1}, {2, 2, 2, 2}};
+
+static int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
+
+int pcg_class_id(int la, int lb, int lc, int ld) {
+  if (la < lb || lc < ld || la > PCG_MAXL || lc > PCG_MAXL) return -1;
+  int pb = pair_class(la, lb), pk = pair_class(lc, ld);
+  if (pb < pk) return -1;
+  return pb * (pb + 1) / 2 + pk;
+}
+
+int pcg_class_nout(int cls) {
+  if (cls < 0 || cls >= 21) return 0;
+  const int* l = kClassL[cls];
+  return (2 * l[0] + 1) * (2 * l[1] + 1) * (2 * l[2] + 1) * (2 * l[3] + 1);
+}
+
+int pcg_launch_eri_g0(int, const DevPairsExt&, const BoysTable&, const int2*, int, double*, int, cudaStream_t);
+int pcg_launch_eri_g1(int, const DevPairsExt&, const BoysTable&, const int2*, int, double*, int, cudaStream_t);
+int pcg_launch_eri_g2(int, const DevPairsExt&, const BoysTable&, const int2*, int, double*, int, cudaStream_t);
+int pcg_launch_eri_g3(int, const DevPairsExt&, const BoysTable&, const int2*, int, double*, int, cudaStream_t);
+int pcg_launch_eri_g4(int, const DevPairsExt&, const BoysTable&, const int2*, int, double*, int, cudaStream_t);
+int pcg_launch_eri_g5(int, const DevPairsExt&, const BoysTable&, const int2*, int, double*, int, cudaStream_t);
+
+int pcg_launch_eri(int cls, const DevBasis& b, const DevPairsExt& pr, const BoysTable& bt, const int2* tasks,
+                   int ntask, double* store, int precision, float, const double*, cudaStream_t s) {
+  (void)b;
+  if (ntask <= 0) return PCG_OK;
+  if (cls < 0 || cls > 20) return PCG_ERR_ARG;
+  if (cls <= 5) return pcg_launch_eri_g0(cls, pr, bt, tasks, ntask, store, precision, s);
+  if (cls <= 13) return pcg_launch_eri_g1(cls, pr, bt, tasks, ntask, store, precision, s);
+  if (cls <= 17) return pcg_launch_eri_g2(cls, pr, bt, tasks, ntask, store, precision, s);
+  if (cls <= 19) return pcg_launch_eri_g3(cls, pr, bt, tasks, ntask, store, precision, s);
+  if (precision == 0) return pcg_launch_eri_g4(cls, pr, bt, tasks, ntask, store, precision, s);
+  return pcg_launch_eri_g5(cls, pr, bt, tasks, ntask, store, precision, s);
+}
+
+#define NS(l) (2 * (l) + 1)
+#define PCG_SHAPE_CASES(X)                                                                               \
+  X(0, 1, 1, 1, 1) X(1, 3, 1, 1, 1) X(2, 3, 1, 3, 1) X(3, 3, 3, 1, 1) X(4, 3, 3, 3, 1) X(5, 3, 3, 3, 3) \
+  X(6, 5, 1, 1, 1) X(7, 5, 1, 3, 1) X(8, 5, 1, 3, 3) X(9, 5, 1, 5, 1) X(10, 5, 3, 1, 1)                 \
+  X(11, 5, 3, 3, 1) X(12, 5, 3, 3, 3) X(13, 5, 3, 5, 1) X(14, 5, 3, 5, 3) X(15, 5, 5, 1, 1)             \
+  X(16, 5, 5, 3, 1) X(17, 5, 5, 3, 3) X(18, 5, 5, 5, 1) X(19, 5, 5, 5, 3) X(20, 5, 5, 5, 5)
+
+int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
+                      const double* store, const double* D, double* G, cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  const int threads = 128, blocks = (ntask + threads - 1) / threads;
+  switch (cls) {
+#define X(id, a, bb, c, d) \
+  case id: k_digest<a, bb, c, d><<<blocks, threads, 0, s>>>(b, pr, tasks, ntask, store, D, G); break;
+    PCG_SHAPE_CASES(X)
+#undef X
+    default: return PCG_ERR_ARG;
+  }
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+int pcg_launch_dense(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
+                     const double* store, double* eri, cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  const int threads = 128, blocks = (ntask + threads - 1) / threads;
+  switch (cls) {
+#define X(id, a, bb, c, d) \
+  case id: k_dense<a, bb, c, d><<<blocks, threads, 0, s>>>(b, pr, tasks, ntask, store, eri); break;
+    PCG_SHAPE_CASES(X)
+#undef X
+    default: return PCG_ERR_ARG;
+  }
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+int pcg_launch_schwarz(int cls, const int2* tasks, int ntask, const double* store, double* Q, cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  const int threads = 128, blocks = (ntask + threads - 1) / threads;
+  switch (cls) {
+    case 0: k_schwarz<1, 1><<<blocks, threads, 0, s>>>(tasks, ntask, store, Q); break;
+    case 2: k_schwarz<3, 1><<<blocks, threads, 0, s>>>(tasks, ntask, store, Q); break;
+    case 5: k_schwarz<3, 3><<<blocks, threads, 0, s>>>(tasks, ntask, store, Q); break;
+    case 9: k_schwarz<5, 1><<<blocks, threads, 0, s>>>(tasks, ntask, store, Q); break;
+    case 14: k_schwarz<5, 3><<<blocks, threads, 0, s>>>(tasks, ntask, store, Q); break;
+    case 20: k_schwarz<5, 5><<<blocks, threads, 0, s>>>(tasks, ntask, store, Q); break;
+    default: return PCG_ERR_ARG;
+  }
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+// ----------------------------------------------------------------------------------
+// Task expansion for one bucket: bra r (sorted by Schwarz factor, descending) pairs
+// with ket positions [qstart[r], qstart[r] + cnt[r] - diag[r]) of the ket list, plus
+// its own pair when diag[r] (the diagonal quartet upstream always computes).
+// ----------------------------------------------------------------------------------
+__global__ void k_expand(int nbra, const int* __restrict__ bra, const int* __restrict__ ket,
+                         const long long* __restrict__ off, const int* __restrict__ qstart,
+                         const int* __restrict__ diag, long long ntask, int2* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  int lo = 0, hi = nbra - 1;  // last r with off[r] <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  const int r = lo;
+  const long long q = t - off[r];
+  const long long cnt = off[r + 1] - off[r];
+  int kp;
+  if (diag[r] && q == cnt - 1) kp = ket[r];
+  else kp = ket[qstart[r] + q];
+  out[t] = make_int2(bra[r], kp);
+}
+
+int pcg_launch_expand(int nbra, const int* bra, const int* ket, const long long* off, const int* qstart,
+                      const int* diag, long long ntask, int2* out, cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  const int threads = 256;
+  const long long blocks = (ntask + threads - 1) / threads;
+  k_expand<<<(unsigned)blocks, threads, 0, s>>>(nbra, bra, ket, off, qstart, diag, ntask, out);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+// F = H + (G + G^T) / 2
+__global__ void k_fock(int n, const double* __restrict__ H, const double* __restrict__ G, double* __restrict__ F) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const int i = idx / n, j = idx % n;
+  F[idx] = H[idx] + 0.5 * (G[idx] + G[(size_t)j * n + i]);
+}
+
+int pcg_launch_fock(int n, const double* H, const double* G, double* F, cudaStream_t s) {
+  if (n <= 0) return PCG_OK;
+  k_fock<<<(n * n + 255) / 256, 256, 0, s>>>(n, H, G, F);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}

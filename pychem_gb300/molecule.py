@@ -1,0 +1,112 @@
+"""Molecule, atoms and shells in upstream AO order.
+
+Follows ``Util/structures.py``: coordinates ``[symbol, Z, x, y, z]`` in Angstrom by
+default (``structures.py:339-360``, ``toBohr`` from ``Data/constants.py:2``); atoms in
+input order, shells in basis-library order (``structures.py:464-492``), spherical
+functions per shell in the rows of ``Data/transform_basis.py:3-12``; electron counts
+``(N +/- (mult-1))/2`` (``structures.py:484-485``).  Contraction coefficients are
+scaled by ``(2a)^{(l+1.5)/2}`` (``ScaledCCs``, ``structures.py:843``) and contracted
+functions are not renormalised, as upstream.
+"""
+import json
+import math
+import os
+
+import numpy as np
+
+TO_BOHR = 1.8897161646320724
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "basis_sets.json")
+N_ELECTRONS = {"H": 1, "HE": 2, "LI": 3, "BE": 4, "B": 5, "C": 6, "N": 7, "O": 8, "F": 9, "NE": 10,
+               "NA": 11, "MG": 12, "AL": 13, "SI": 14, "P": 15, "S": 16, "CL": 17, "AR": 18}
+MAX_L = 2
+
+_basis_cache = None
+
+
+def basis_library():
+    global _basis_cache
+    if _basis_cache is None:
+        with open(DATA) as fh:
+            _basis_cache = json.load(fh)
+    return _basis_cache
+
+
+def clean_basis_name(name):
+    """Upstream remove_punctuation (Util/structures.py:972-974)."""
+    return name.replace("*", "s").replace("-", "").replace("(", "").replace(")", "").replace(",", "").upper()
+
+
+def pure_norm(l):
+    """Normalisation of the pure-axis Cartesian component x^l (ContractionScaling)."""
+    return (math.gamma(l + 0.5) * math.gamma(0.5) ** 2) ** -0.5
+
+
+class Molecule:
+    def __init__(self, coords, basis="STO-3G", charge=0, multiplicity=1, units="ANGSTROM"):
+        scale = TO_BOHR if units.upper() == "ANGSTROM" else 1.0
+        self.Basis = clean_basis_name(basis)
+        lib = basis_library()
+        if self.Basis not in lib:
+            raise ValueError("basis set %s not available (have %s)" % (basis, sorted(lib)))
+        data = lib[self.Basis]
+        self.Charge = charge
+        self.Multiplicity = multiplicity
+        self.atoms = []
+        for row in coords:
+            sym = str(row[0]).upper()
+            self.atoms.append((sym, float(row[1]), np.array([float(v) * scale for v in row[2:5]])))
+        self.NAtom = len(self.atoms)
+        shells = []
+        for ia, (sym, Z, xyz) in enumerate(self.atoms):
+            if sym not in data:
+                raise ValueError("element %s not in basis %s" % (sym, self.Basis))
+            for fn in data[sym]:
+                l = int(fn[0])
+                if l > MAX_L:
+                    raise NotImplementedError("shells above d are not supported (l=%d)" % l)
+                exps = np.array([p[0] for p in fn[1:]], dtype=np.float64)
+                ccs = np.array([p[1] for p in fn[1:]], dtype=np.float64)
+                shells.append((l, exps, ccs, ia))
+        self.shells = shells
+        self.NCgtf = len(shells)
+        ao = 0
+        self.sh_ao = []
+        for s in shells:
+            self.sh_ao.append(ao)
+            ao += 2 * s[0] + 1
+        self.NOrbitals = ao
+        self.NElectrons = sum(N_ELECTRONS[a[0]] for a in self.atoms) - charge
+        self.NAlphaElectrons = (self.NElectrons + (multiplicity - 1)) // 2
+        self.NBetaElectrons = (self.NElectrons - (multiplicity - 1)) // 2
+        if self.NAlphaElectrons - self.NBetaElectrons + 1 != multiplicity or \
+                self.NAlphaElectrons + self.NBetaElectrons != self.NElectrons:
+            raise ValueError("charge and multiplicity inconsistent with specified molecule")
+
+    # -- flat arrays for the device ---------------------------------------------------
+    def arrays(self):
+        sh_l = np.array([s[0] for s in self.shells], dtype=np.int32)
+        sh_nprim = np.array([len(s[1]) for s in self.shells], dtype=np.int32)
+        sh_prim = np.concatenate([[0], np.cumsum(sh_nprim)[:-1]]).astype(np.int32)
+        sh_ao = np.array(self.sh_ao, dtype=np.int32)
+        sh_atom = np.array([s[3] for s in self.shells], dtype=np.int32)
+        sh_xyz = np.array([self.atoms[s[3]][2] for s in self.shells], dtype=np.float64).reshape(-1, 3)
+        pr_exp = np.concatenate([s[1] for s in self.shells])
+        pr_cc = np.concatenate([s[2] * (2.0 * s[1]) ** ((s[0] + 1.5) / 2.0) * pure_norm(s[0]) for s in self.shells])
+        at_xyz = np.array([a[2] for a in self.atoms], dtype=np.float64).reshape(-1, 3)
+        at_z = np.array([a[1] for a in self.atoms], dtype=np.float64)
+        return dict(sh_l=sh_l, sh_nprim=sh_nprim, sh_prim=sh_prim, sh_ao=sh_ao, sh_atom=sh_atom,
+                    sh_xyz=np.ascontiguousarray(sh_xyz), pr_exp=pr_exp, pr_cc=pr_cc,
+                    at_xyz=np.ascontiguousarray(at_xyz), at_z=at_z)
+
+    def nuclear_repulsion(self):
+        """Methods/integrals.py:196-207."""
+        e = 0.0
+        for i in range(self.NAtom):
+            for j in range(i):
+                r = float(np.linalg.norm(self.atoms[i][2] - self.atoms[j][2]))
+                e += self.atoms[i][1] * self.atoms[j][1] / r
+        return e
+
+    def coords_list(self, units="BOHR"):
+        s = 1.0 if units.upper() == "BOHR" else 1.0 / TO_BOHR
+        return [[a[0], a[1]] + list(a[2] * s) for a in self.atoms]
