@@ -1,0 +1,384 @@
+"""Benchmark: plain-FP64 direct RHF + MP2 of a 16-water cluster in 6-31G on one GB300.
+
+Workload (the configuration the headline metric is quoted on): (H2O)16 on a 4x2x2 grid
+with 2.9 A spacing, seeded random rotations and N(0, 0.05 A) jitter, 6-31G, 208 AO,
+80 doubly occupied orbitals (pychem_gb300.workloads.water_cluster, seed 2026).
+
+One step = one complete solve from device-resident shells: primitive-pair data,
+S/T/V, Schwarz pass, screened quartet lists, every screened ERI into the in-core
+store, SCF to |dE| < 1e-10 Eh and D-RMS < 1e-8, then the MP2 AO->MO transform and
+energy.  `value` is the time of that step (time-to-convergence incl. MP2, seconds,
+CUDA events, L2 flushed between steps); `e2e` is the same solve through the public
+call pychem_gb300.api.rhf_mp2 from host coordinates to host results.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "RHF time-to-convergence & ERI quartets/s on 1 GB300, learned/mixed vs plain FP64 @1e-8 Eh"
+WORKLOAD = "(H2O)16 water cluster, 6-31G, 208 AO, RHF + MP2"
+SEED = 2026
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
+# ------------------------------------------------------------------------------------
+# CPU side (oracle port): shared by the cpu_baseline leg and the reference arm
+# ------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    atoms, basis, quads = args
+    import ctypes
+    import numpy as np
+    from oracle import oracle as O
+    b = O.Basis(atoms, basis)
+    q = np.ascontiguousarray(np.asarray(quads, dtype=np.int32).reshape(-1))
+    t0 = time.perf_counter()
+    O.lib().oracle_eri_list(b.c, len(quads), q.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return time.perf_counter() - t0
+
+
+_PLAN = {}
+
+
+def cpu_plan(atoms, basis, rng):
+    """Schwarz pass and screened-quartet count on the CPU oracle; returns
+    (total screened quartets, sampler).  Cached per molecule."""
+    import numpy as np
+    from oracle import oracle as O
+    key = (basis, tuple(tuple(a[2:]) for a in atoms))
+    if key not in _PLAN:
+        b = O.Basis(atoms, basis)
+        Q = b.schwarz()
+        ia, ib = np.triu_indices(b.nshell)
+        q = Q[ia, ib]
+        thr = O.INTEGRAL_THRESHOLD
+        order = np.argsort(-q)
+        qs = q[order]
+        # row i (sorted order) pairs with j <= i when q_i q_j > thr, plus its own diagonal
+        cpre = np.empty(len(qs), dtype=np.int64)
+        for i in range(len(qs)):
+            cpre[i] = min(i + 1, np.searchsorted(-qs[: i + 1] * qs[i], -thr, side="left"))
+        cnt = cpre + (cpre <= np.arange(len(qs)))
+        _PLAN[key] = (ia, ib, order, cpre, cnt, int(cnt.sum()))
+    ia, ib, order, cpre, cnt, total = _PLAN[key]
+
+    def sample(n):
+        rows = rng.choice(len(cnt), size=n, p=cnt / total)
+        j = (rng.random(n) * cnt[rows]).astype(np.int64)
+        j = np.where(j >= cpre[rows], rows, j)
+        p1, p2 = order[rows], order[j]
+        return np.stack([ia[p1], ib[p1], ia[p2], ib[p2]], axis=1).astype(np.int32)
+    return total, sample, None
+
+
+def cpu_eri_rate(atoms, basis, workers, target_s=10.0, seed=SEED):
+    """Screened quartets/s of the CPU oracle on a bounded random sample; returns
+    (quartets_per_s, total_quartets, sample_description, cores)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    total, sample, _ = cpu_plan(atoms, basis, rng)
+    probe = sample(2000)
+    t = _cpu_worker((atoms, basis, probe))
+    per = t / len(probe)
+    n = int(min(total, max(2000, target_s / per * workers)))
+    quads = sample(n)
+    if workers == 1:
+        wall = _cpu_worker((atoms, basis, quads))
+    else:
+        chunks = [quads[k::workers] for k in range(workers)]
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(workers) as pool:
+            # each worker times its own kernel loop (process start-up excluded); the
+            # slowest worker bounds the parallel wall time
+            wall = max(pool.map(_cpu_worker, [(atoms, basis, c) for c in chunks]))
+    rate = n / wall
+    desc = "%d of %d screened shell quartets (uniform sample) through the C oracle port on %d core(s), %.1f s" % (
+        n, total, workers, wall)
+    return rate, total, desc
+
+
+def reference_arm(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    from pychem_gb300 import workloads as W
+    atoms_ang = W.water_cluster(seed=SEED)
+    atoms = [(a[0], a[1], a[2] * 1.8897161646320724, a[3] * 1.8897161646320724, a[4] * 1.8897161646320724)
+             for a in atoms_ang]
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    vals = []
+    desc = ""
+    for k in range(args.warmup + args.steps):
+        rate, total, desc = cpu_eri_rate(atoms, "6-31G", cores, target_s=4.0, seed=SEED + k)
+        if k >= args.warmup:
+            vals.append(total / rate)
+    v = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "basis": "6-31G", "seed": SEED},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                             "sample": desc + "; value = ERI phase extrapolated to every screened quartet "
+                                              "(a lower bound on the CPU time-to-convergence: SCF and MP2 not added)"},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------
+class Clocks:
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0])); mx.append(float(r[1]))
+                for nm, v in zip(names, r[3:7]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def probe_peak(torch, _lib, fp32):
+    import ctypes
+    blocks, threads, iters = 152 * 8, 256, 4096
+    out = torch.empty(blocks * threads, dtype=torch.float32 if fp32 else torch.float64, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    best = 0.0
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.call("pcg_fma_probe", blocks, threads, iters, 1 if fp32 else 0, ctypes.c_void_p(out.data_ptr()), s)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = max(best, blocks * threads * iters * 8 * 2 / (ms * 1e-3) / 1e12)
+    return best
+
+
+def gpu_arm(args):
+    import numpy as np
+    import torch
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from pychem_gb300 import _lib, workloads as W
+    from pychem_gb300.api import rhf_mp2
+    from pychem_gb300.engine import GpuEngine
+    from pychem_gb300.molecule import Molecule
+    from pychem_gb300.scf import mp2_flops, rhf, rmp2
+
+    coords = W.water_cluster(seed=SEED)
+    mol = Molecule(coords, "6-31G")
+    n, o = mol.NOrbitals, mol.NAlphaElectrons
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def solve(eng):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        ev[0].record()
+        eng.compute_pair_data()
+        eng.one_electron(); eng.schwarz(); eng.build_tasks()
+        ev[1].record()
+        eng.compute_eris()
+        ev[2].record()
+        r = rhf(eng)
+        ev[3].record()
+        e2 = rmp2(eng, r.C, r.eps)
+        ev[4].record()
+        return r, e2, ev
+
+    def run(precision, k_steps, warm):
+        eng = GpuEngine(mol, precision=precision)
+        for _ in range(warm):
+            solve(eng)
+        times, phases, res = [], [], None
+        launches0 = _lib.launch_count
+        for _ in range(k_steps):
+            flush.zero_()
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r, e2, ev = solve(eng)
+            e1.record()
+            barrier()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            phases.append([ev[i].elapsed_time(ev[i + 1]) / 1e3 for i in range(4)])
+            res = (r, e2)
+        launches = (_lib.launch_count - launches0) / max(1, k_steps)
+        return eng, times, phases, res, launches
+
+    peaks = load_peaks()
+    fp64_peak = probe_peak(torch, _lib, False)
+    fp32_peak = probe_peak(torch, _lib, True)
+
+    with Clocks(local) as clk:
+        eng, times, phases, (r, e2), launches = run("fp64", args.steps, args.warmup)
+    clocks = clk.summary()
+    # mixed precision: same solve, quartets below the 1e-4 Schwarz bound in FP32
+    engm, times_m, phases_m, (rm, e2m), _ = run("mixed", max(1, args.steps), 1)
+
+    t_step = statistics.mean(times)
+    ph = [statistics.mean(p[i] for p in phases) for i in range(4)]
+    ops = {s["cls"]: s for s in json.load(open(os.path.join(REPO, "pychem_gb300", "csrc", "eri_ops.json")))}
+    names = list(ops)
+    eri_flops = 0.0
+    for (cls, part), npq in eng.prim_quartets.items():
+        st = ops[names[cls]]
+        nq = eng.classes[cls][part][1]
+        eri_flops += float(npq) * (st["vrr_flops"] + st["overhead_flops"]) + nq * st["finish_flops"]
+    quartets = eng.stats["quartets"]
+    # Fock builds in isolation (digestion + symmetrisation)
+    D = r.D.contiguous()
+    fk = []
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(); eng.fock(D); b.record(); torch.cuda.synchronize()
+        fk.append(a.elapsed_time(b) / 1e3)
+    t_fock = min(fk)
+    # ERI pass alone (for the roofline of the dominant kernels)
+    eri_t = []
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(); eng.compute_eris(); b.record(); torch.cuda.synchronize()
+        eri_t.append(a.elapsed_time(b) / 1e3)
+    t_eri = min(eri_t)
+    store_bytes = sum(s.numel() * 8 for s in eng.stores.values())
+
+    # end to end through the public API with host buffers
+    e2e_t = []
+    for k in range(max(1, args.steps)):
+        flush.zero_()
+        barrier()
+        t0 = time.perf_counter()
+        out = rhf_mp2(coords, "6-31G")
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    t_e2e = statistics.mean(e2e_t)
+
+    # max over ranks
+    if world > 1:
+        tt = torch.tensor([t_step, t_e2e], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        return
+
+    cpu = None
+    if world == 1:
+        atoms_b = [(a[0], a[1], *a[2]) for a in mol.atoms]
+        rate, total, desc = cpu_eri_rate(atoms_b, "6-31G", 1, target_s=12.0)
+        cpu = {"value": total / rate, "unit": "s", "cores": 1, "kind": "port",
+               "sample": desc + "; value = ERI phase extrapolated to every screened quartet (SCF and MP2 not added)",
+               "eri_quartets_per_s": rate}
+
+    achieved = eri_flops / t_eri / 1e12
+    line = {
+        "metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "basis": "6-31G", "nbf": n, "n_occ": o, "seed": SEED,
+                   "screening": "Schwarz 1e-8", "scf": "|dE|<1e-10 and D-RMS<1e-8, DIIS(10)",
+                   "l2": "256 MiB buffer written between steps", "parallelism": "replicas" if world > 1 else "single"},
+        "E_rhf": r.E, "E_mp2_total": r.E + e2, "scf_iterations": r.iterations,
+        "eri_shell_quartets": quartets,
+        "eri_quartets_per_s": quartets / t_eri,
+        "fock_builds_per_s": 1.0 / t_fock,
+        "mp2_tflops": mp2_flops(n, o, n - o) / ph[3] / 1e12,
+        "phases_s": {"setup_1e_schwarz_tasks": ph[0], "eri": ph[1], "scf": ph[2], "mp2": ph[3]},
+        "mixed": {"value": statistics.mean(times_m), "unit": "s", "fp32_below": 1e-4,
+                  "quartets_fp32": engm.stats["quartets_fp32"], "quartets_fp64": engm.stats["quartets_fp64"],
+                  "dE_rhf_vs_fp64": rm.E - r.E, "dE_mp2_vs_fp64": (rm.E + e2m) - (r.E + e2),
+                  "eri_s": statistics.mean(p[1] for p in phases_m)},
+        "roofline": {"bound": "fp64", "kernel": "ERI class kernels k_eri<*> (FP64 pipe)",
+                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                     "peak_source": "measured by bench.py FP64 FMA probe (pcg_fma_probe)",
+                     "traffic": None, "algorithmic_flops": eri_flops, "eri_pass_s": t_eri},
+        "peaks": {"fp64_tflops_probe": fp64_peak, "fp32_tflops_probe": fp32_peak,
+                  "hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")},
+        "fock_digest": {"s_per_build": t_fock, "store_bytes": store_bytes,
+                        "hbm_frac": store_bytes / t_fock / 1e9 / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None},
+        "cpu_baseline": cpu,
+        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": out["h2d_bytes"],
+                "d2h_bytes_per_step": out["d2h_bytes"]},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

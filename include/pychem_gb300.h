@@ -179,6 +179,11 @@ int pcg_fock_build(int n, const double *H, const double *G, double *F, void *str
 int pcg_dense_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                     int ntask, const double *store, double *eri, void *stream);
 
+/* Arithmetic-throughput probe (measurement support, no upstream counterpart): blocks x
+ * threads threads each run 8 independent FMA chains of `iters` steps in FP64 (fp32 = 0)
+ * or FP32, writing one value per thread to `out` (blocks*threads elements). */
+int pcg_fma_probe(int blocks, int threads, int iters, int fp32, void *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

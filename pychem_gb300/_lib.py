@@ -63,7 +63,16 @@ _SIGS = {
     "pcg_fock_build": [c_int, c_void_p, c_void_p, c_void_p, c_void_p],
     "pcg_dense_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p,
                         c_void_p, c_void_p],
+    "pcg_fma_probe": [c_int, c_int, c_int, c_int, c_void_p, c_void_p],
 }
+# entry points that launch exactly one kernel of this library per call
+LAUNCHERS = {"pcg_pair_data", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
+             "pcg_digest_class", "pcg_fock_build", "pcg_dense_class", "pcg_fma_probe",
+             "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",
+             "pcg_two_electron_vrr", "pcg_two_electron_contract", "pcg_two_electron_hrr",
+             "pcg_one_electron_fundamentals", "pcg_one_electron_vrr", "pcg_one_electron_hrr",
+             "pcg_one_electron_kinetic", "pcg_one_electron_contract"}
+launch_count = 0
 _RESTYPES = {"pcg_last_error": ctypes.c_char_p}
 
 _lib = None
@@ -96,6 +105,9 @@ def check(rc, what=""):
 
 
 def call(name, *args):
+    global launch_count
+    if name in LAUNCHERS:
+        launch_count += 1
     rc = getattr(load(), name)(*args)
     check(rc, name)
     return rc

@@ -112,3 +112,31 @@ int pcg_dense_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Arithmetic-throughput probe: each thread runs 8 independent FMA chains for `iters`
+// steps (FP64 when fp32 == 0, else FP32); the result is written so the work is kept.
+// Used by bench.py to measure the FP64/FP32 pipe peaks that the ERI roofline uses.
+// ---------------------------------------------------------------------------------
+template <class T>
+__global__ void k_fma_probe(int iters, T* out) {
+  T a0 = (T)threadIdx.x * (T)1e-3, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
+  T a4 = a0 + (T)4, a5 = a0 + (T)5, a6 = a0 + (T)6, a7 = a0 + (T)7;
+  const T m = (T)0.999999, c = (T)1e-7;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+extern "C" int pcg_fma_probe(int blocks, int threads, int iters, int fp32, void* out, void* stream) {
+  if (blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0 || !out) {
+    pcg_set_error("pcg_fma_probe: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  if (fp32) k_fma_probe<float><<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (float*)out);
+  else k_fma_probe<double><<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (double*)out);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}

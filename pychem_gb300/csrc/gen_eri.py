@@ -257,6 +257,25 @@ def gen_sph(la, lb, lc, ld, cart, em, ctype="double"):
     return out
 
 
+def count_flops(lines):
+    """Floating-point operations of emitted statements: FMA = 2, MUL/ADD = 1."""
+    total = 0
+    for line in lines:
+        total += 2 * line.count("fma(")
+        total += line.count(" * ")
+        total += line.count(" += ")
+    return total
+
+
+def overhead_flops(L):
+    """Per primitive quartet, outside the VRR (see k_eri in eri_kernels.cuh): P-Q (3),
+    zeta+eta (1), Newton rsqrt (9), 1/(zeta+eta) (1), rho (2), T (6), Boys top order
+    (2 + 7 FMA), prefactor (2), scaling F_0..F_L (L+1); for L > 0 also exp(-T) (7 FMA
+    + 2), downward recursion (3 per order) and the W-P, W-Q, 1/2(zeta+eta), rho/zeta,
+    rho/eta factors (11)."""
+    return 41 + L if L == 0 else 68 + 4 * L
+
+
 def gen_class(la, lb, lc, ld, ctype="double", suffix=""):
     """Returns (source, stats) for the device functions of one class."""
     tag = "%d%d%d%d" % (la, lb, lc, ld)
@@ -310,7 +329,10 @@ def gen_class(la, lb, lc, ld, ctype="double", suffix=""):
         src.append("    out(%d, %s);" % (i, name))
     src.append("  }")
     src.append("};")
+    acc_lines = ["acc += v"] * nacc
     stats = dict(cls=tag, L=L, nacc=nacc, vrr_ops=vrr_flop + nacc, finish_ops=em2.nflop,
+                 vrr_flops=count_flops(vrr_lines) + nacc, finish_flops=count_flops(em2.lines),
+                 overhead_flops=overhead_flops(L),
                  nout=(2 * la + 1) * (2 * lb + 1) * (2 * lc + 1) * (2 * ld + 1))
     return "\n".join(src), stats
 

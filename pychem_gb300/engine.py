@@ -95,9 +95,6 @@ class GpuEngine:
                        Kf=torch.empty(tot, dtype=torch.float32, device=dv),
                        oo2z=torch.empty(tot, dtype=torch.float64, device=dv))
         p = self.pd
-        _lib.call("pcg_pair_data", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ppoff"]),
-                  _ptr(p["AB"]), _ptr(p["zeta"]), _ptr(p["P"]), _ptr(p["PA"]), _ptr(p["K"]), _ptr(p["Kf"]),
-                  _ptr(p["oo2z"]), _stream())
         t = PairsT()
         t.npair = self.npair; t.npp = tot
         for k, f in (("A", "A"), ("B", "B"), ("ppoff", "ppoff"), ("npp", "npp_of"), ("AB", "AB"), ("zeta", "zeta"),
@@ -111,6 +108,14 @@ class GpuEngine:
         self.kinds = [tuple(int(x) for x in uniq[i]) for i in order]
         kind_index = {k: i for i, k in enumerate(self.kinds)}
         self.pair_kind = np.array([kind_index[tuple(int(x) for x in r)] for r in keys], dtype=np.int32)
+        self.compute_pair_data()
+
+    def compute_pair_data(self):
+        """Primitive-pair data from the device-resident shells (one kernel)."""
+        p = self.pd
+        _lib.call("pcg_pair_data", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ppoff"]),
+                  _ptr(p["AB"]), _ptr(p["zeta"]), _ptr(p["P"]), _ptr(p["PA"]), _ptr(p["K"]), _ptr(p["Kf"]),
+                  _ptr(p["oo2z"]), _stream())
 
     # ---------------------------------------------------------------------------------
     def one_electron(self):
@@ -222,6 +227,13 @@ class GpuEngine:
             self.classes[cls] = rec
             nq64 += rec.get("64", (None, 0))[1]
             nq32 += rec.get("32", (None, 0))[1]
+        # primitive quartets per class and part (for the algorithmic flop count)
+        self.prim_quartets = {}
+        npp = self.pd["npp"].to(torch.int64)
+        for cls, rec in self.classes.items():
+            for part, (tasks, n) in rec.items():
+                tv = tasks.view(n, 2).to(torch.int64)
+                self.prim_quartets[(cls, part)] = (npp[tv[:, 0]] * npp[tv[:, 1]]).sum()
         self.stats["quartets_fp64"] = nq64
         self.stats["quartets_fp32"] = nq32
         self.stats["quartets"] = nq64 + nq32
@@ -238,8 +250,10 @@ class GpuEngine:
                 self.stores[(cls, part)] = store
         return self.stores
 
-    def prepare(self):
+    def prepare(self, recompute_pairs=False):
         """One-electron matrices, Schwarz factors, task lists and ERI store."""
+        if recompute_pairs:
+            self.compute_pair_data()
         self.one_electron()
         self.schwarz()
         self.build_tasks()
