@@ -32,7 +32,7 @@ def basis_library():
 
 
 def clean_basis_name(name):
-    """Upstream remove_punctuation (Util/structures.py:972-974)."""
+    """Upstream remove_punctuation (Util/structures.py:975-977)."""
     return name.replace("*", "s").replace("-", "").replace("(", "").replace(")", "").replace(",", "").upper()
 
 

@@ -1,0 +1,56 @@
+"""Run one phase of a benchmark workload, for profiling (ncu) on a bounded case.
+
+    python -m pychem_gb300.profile_case --case water16 --phase eri [--repeat 2]
+
+cases:  water16 ((H2O)16 / 6-31G, 208 AO), water4 ((H2O)4 / 6-31G), alkane12
+        (C12H26 / cc-pVDZ, 298 AO)
+phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2)
+"""
+import argparse
+import time
+
+import torch
+
+from . import workloads as W
+from .engine import GpuEngine
+from .molecule import Molecule
+from .scf import rhf, rmp2
+
+CASES = {
+    "water16": lambda: Molecule(W.water_cluster(), "6-31G"),
+    "water4": lambda: Molecule(W.water_cluster(nx=2, ny=2, nz=1), "6-31G"),
+    "alkane12": lambda: Molecule(W.alkane(12), "cc-pVDZ"),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="water16", choices=sorted(CASES))
+    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--repeat", type=int, default=1)
+    args = ap.parse_args()
+    mol = CASES[args.case]()
+    eng = GpuEngine(mol, precision=args.precision)
+    eng.one_electron(); eng.schwarz(); eng.build_tasks(); eng.compute_eris()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.repeat):
+        if args.phase == "eri":
+            eng.compute_eris()
+        elif args.phase == "fock":
+            n = eng.nbf
+            eng.fock(torch.eye(n, dtype=torch.float64, device="cuda") * 0.1)
+        elif args.phase == "scf":
+            r = rhf(eng)
+        else:
+            r = rhf(eng)
+            rmp2(eng, r.C, r.eps)
+    torch.cuda.synchronize()
+    print("%s %s %s: %.4f s per repeat, %d quartets" % (args.case, args.phase, args.precision,
+                                                         (time.perf_counter() - t0) / args.repeat,
+                                                         eng.stats["quartets"]))
+
+
+if __name__ == "__main__":
+    main()
