@@ -174,6 +174,21 @@ int pcg_digest_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs
                      int ntask, const double *store, const double *D, double *G, void *stream);
 int pcg_fock_build(int n, const double *H, const double *G, double *F, void *stream);
 
+/* No counterpart in the upstream code.  The same Fock build as pcg_digest_class over
+ * nclass classes followed by pcg_fock_build, for callers that cannot allocate device
+ * memory (their GPU memory belongs to another allocator or to a pool fixed at
+ * start-up): the nbf x nbf accumulator lives in a static device array inside the
+ * library, so the caller passes only inputs (H, D, per class: class id, task list,
+ * task count, store -- host arrays of device pointers) and the output F.
+ * Limit: nbf <= 512 (2 MiB held on every GPU that loads the library); larger nbf
+ * returns PCG_ERR_CAPACITY.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) and should come before any stream capture.  Calls
+ * share the array; calls that overlap on the GPU race and must be serialised. */
+int pcg_fock_build_noalloc(const pcg_basis_t *basis, const pcg_pairs_t *pairs, int nclass,
+                           const int *cls, const int *const *tasks, const int *ntask,
+                           const double *const *stores, const double *H, const double *D, double *F,
+                           void *stream);
+
 /* Scatter the stored blocks of one class into a dense nbf^4 tensor with the 8-fold
  * symmetry (Methods/hartree_fock.py:314-325). */
 int pcg_dense_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,

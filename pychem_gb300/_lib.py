@@ -64,6 +64,8 @@ _SIGS = {
     "pcg_dense_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p,
                         c_void_p, c_void_p],
     "pcg_fma_probe": [c_int, c_int, c_int, c_int, c_void_p, c_void_p],
+    "pcg_fock_build_noalloc": [ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_int, c_void_p, c_void_p, c_void_p,
+                               c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
 }
 # entry points that launch exactly one kernel of this library per call
 LAUNCHERS = {"pcg_pair_data", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",

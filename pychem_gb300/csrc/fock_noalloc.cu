@@ -1,0 +1,88 @@
+// Closed-shell Fock build that allocates no device memory.
+//
+// The ordinary path (pcg_digest_class per class + pcg_fock_build) needs a caller-
+// allocated nbf x nbf accumulator G.  Some callers cannot allocate device memory at
+// the point where they build a Fock matrix: hosts whose GPU memory is owned by
+// another allocator (a framework's caching allocator, or one fixed pool reserved at
+// start-up) that gives this library no allocation hook, and hosts that forbid any
+// allocation after initialisation.  For them the accumulator lives in the file-scope
+// array below, sized for nbf <= PCG_NOALLOC_MAX_NBF (512 basis functions, 2 MiB).
+// Every GPU that loads this library holds that array until the process exits.
+//
+// The array is a device symbol: in host code its name is only a stand-in, so the
+// host obtains its device address with cudaGetSymbolAddress, once per device, with
+// that device current, on the first call made on that device.  That first call
+// should therefore come before any stream capture.  Calls share the one array: each
+// call clears it before use, and calls that overlap on the GPU (two streams, or two
+// host threads on one device) race on it and must be serialised by the caller.
+#include <stdio.h>
+
+#include "../../include/pychem_gb300.h"
+#include "common.cuh"
+#include "pcg_internal.h"
+
+#define PCG_NOALLOC_MAX_NBF 512
+
+static __device__ __align__(256) double g_fock_scratch[PCG_NOALLOC_MAX_NBF * PCG_NOALLOC_MAX_NBF];
+
+static double* g_fock_scratch_addr[64];  // device address per device ordinal
+
+int pcg_launch_fock(int n, const double* H, const double* G, double* F, cudaStream_t s);
+
+static DevBasis basis_of(const pcg_basis_t* b) {
+  DevBasis d;
+  d.nshell = b->nshell; d.nprim = b->nprim; d.natom = b->natom; d.nbf = b->nbf;
+  d.sh_l = b->sh_l; d.sh_nprim = b->sh_nprim; d.sh_prim = b->sh_prim; d.sh_ao = b->sh_ao;
+  d.sh_atom = b->sh_atom; d.sh_xyz = b->sh_xyz; d.pr_exp = b->pr_exp; d.pr_cc = b->pr_cc;
+  d.at_xyz = b->at_xyz; d.at_z = b->at_z;
+  return d;
+}
+
+static DevPairsExt pairs_of(const pcg_pairs_t* p) {
+  DevPairsExt d;
+  d.p.npair = p->npair; d.p.npp = p->npp;
+  d.p.A = p->A; d.p.B = p->B; d.p.ppoff = p->ppoff; d.p.npp_of = p->npp_of;
+  d.p.AB = p->AB; d.p.zeta = p->zeta; d.p.P = p->P; d.p.PA = p->PA; d.p.K = p->K; d.p.Kf = p->Kf;
+  d.oo2z = p->oo2z;
+  return d;
+}
+
+extern "C" int pcg_fock_build_noalloc(const pcg_basis_t* basis, const pcg_pairs_t* pairs, int nclass,
+                                      const int* cls, const int* const* tasks, const int* ntask,
+                                      const double* const* stores, const double* H, const double* D, double* F,
+                                      void* stream) {
+  if (!basis || !pairs || nclass < 0 || (nclass > 0 && (!cls || !tasks || !ntask || !stores)) || !H || !D || !F) {
+    pcg_set_error("pcg_fock_build_noalloc: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  const int n = basis->nbf;
+  if (n <= 0 || n > PCG_NOALLOC_MAX_NBF) {
+    char msg[160];
+    snprintf(msg, sizeof(msg), "pcg_fock_build_noalloc: nbf = %d exceeds the static scratch limit of %d basis functions",
+             n, PCG_NOALLOC_MAX_NBF);
+    pcg_set_error(msg);
+    return PCG_ERR_CAPACITY;
+  }
+  int dev = 0;
+  PCG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { pcg_set_error("pcg_fock_build_noalloc: device ordinal out of range"); return PCG_ERR_ARG; }
+  if (!g_fock_scratch_addr[dev]) {
+    double* p = nullptr;
+    PCG_CUDA(cudaGetSymbolAddress((void**)&p, g_fock_scratch));
+    g_fock_scratch_addr[dev] = p;
+  }
+  double* G = g_fock_scratch_addr[dev];
+  cudaStream_t s = (cudaStream_t)stream;
+  PCG_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * (size_t)n * n, s));
+  const DevBasis b = basis_of(basis);
+  const DevPairsExt pr = pairs_of(pairs);
+  for (int k = 0; k < nclass; ++k) {
+    if (cls[k] < 0 || cls[k] > 20 || ntask[k] < 0) {
+      pcg_set_error("pcg_fock_build_noalloc: bad class entry");
+      return PCG_ERR_ARG;
+    }
+    int rc = pcg_launch_digest(cls[k], b, pr, (const int2*)tasks[k], ntask[k], stores[k], D, G, s);
+    if (rc) return rc;
+  }
+  return pcg_launch_fock(n, H, G, F, s);
+}
