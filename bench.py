@@ -315,6 +315,12 @@ def gpu_arm(args):
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
     t_e2e = statistics.mean(e2e_t)
+    # cross-check of the tensor-core MP2 transform against cuBLAS DGEMM (untimed)
+    e2_fp64 = rmp2(eng, r.C, r.eps, gemm="fp64")
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(); rmp2(eng, r.C, r.eps, gemm="fp64"); b.record(); torch.cuda.synchronize()
+    t_mp2_fp64 = a.elapsed_time(b) / 1e3
 
     # max over ranks
     if world > 1:
@@ -345,6 +351,9 @@ def gpu_arm(args):
         "eri_quartets_per_s": quartets / t_eri,
         "fock_builds_per_s": 1.0 / t_fock,
         "mp2_tflops": mp2_flops(n, o, n - o) / ph[3] / 1e12,
+        "mp2": {"gemm": "BF16 tensor cores, Ozaki split, 6 slices", "s": ph[3],
+                "dE_vs_fp64_dgemm": e2 - e2_fp64, "fp64_dgemm_s": t_mp2_fp64,
+                "fp64_dgemm_tflops": mp2_flops(n, o, n - o) / t_mp2_fp64 / 1e12},
         "phases_s": {"setup_1e_schwarz_tasks": ph[0], "eri": ph[1], "scf": ph[2], "mp2": ph[3]},
         "mixed": {"value": statistics.mean(times_m), "unit": "s", "fp32_below": 1e-4,
                   "quartets_fp32": engm.stats["quartets_fp32"], "quartets_fp64": engm.stats["quartets_fp64"],

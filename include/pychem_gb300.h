@@ -19,6 +19,8 @@
 #ifndef PYCHEM_GB300_H
 #define PYCHEM_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -193,6 +195,24 @@ int pcg_fock_build_noalloc(const pcg_basis_t *basis, const pcg_pairs_t *pairs, i
  * symmetry (Methods/hartree_fock.py:314-325). */
 int pcg_dense_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                     int ntask, const double *store, double *eri, void *stream);
+
+/* FP64-accurate batched GEMM on BF16 tensor cores by error-free operand splitting
+ * (Ozaki scheme; no upstream counterpart -- it carries the AO->MO transform of
+ * Methods/mp2.py:43-69).  Row-major semantics with element strides:
+ *   C[b][m][n] (+)= sum_k A[b*sAb + m*sAm + k*sAk] * B[b*sBb + k*sBk + n*sBn],
+ * C rows contiguous (ldc = N), batch stride sCb; a batch stride of 0 broadcasts.
+ * Each operand needs a unit stride along m or k (A) and n or k (B).  nslice (1..7)
+ * 7-bit slices per operand; exact FP32 level sums need K * (nslice + 2) < 4096.
+ * workspace: pcg_ozaki_workspace() bytes, caller-owned device memory. */
+typedef struct {
+  int batch, M, N, K;
+  long long sAb, sAm, sAk;
+  long long sBb, sBn, sBk;
+  long long sCb;
+} pcg_gemm_desc_t;
+size_t pcg_ozaki_workspace(const pcg_gemm_desc_t *desc, int nslice);
+int pcg_ozaki_gemm(const pcg_gemm_desc_t *desc, const double *A, const double *B, double *C, int nslice,
+                   int accumulate, void *workspace, size_t ws_bytes, void *stream);
 
 /* Arithmetic-throughput probe (measurement support, no upstream counterpart): blocks x
  * threads threads each run 8 independent FMA chains of `iters` steps in FP64 (fp32 = 0)

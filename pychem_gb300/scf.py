@@ -108,24 +108,62 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                      converged=converged, history=history, fock_builds=it, t_fock=t_fock)
 
 
-def rmp2(engine, C, eps, eri=None):
+def ozaki_gemm(A, B, C, batch, M, N, K, sA, sB, sCb, nslice=6, accumulate=False):
+    """C[b][m][n] (+)= sum_k A[b,m,k] B[b,k,n] in FP64 accuracy on BF16 tensor cores
+    (pcg_ozaki_gemm); sA = (sAb, sAm, sAk), sB = (sBb, sBk, sBn) element strides."""
+    import ctypes
+    from . import _lib
+    d = _lib.GemmDescT(batch, M, N, K, sA[0], sA[1], sA[2], sB[0], sB[2], sB[1], sCb)
+    nbytes = _lib.load().pcg_ozaki_workspace(ctypes.byref(d), nslice)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=C.device)
+    _lib.call("pcg_ozaki_gemm", ctypes.byref(d), ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
+              ctypes.c_void_p(C.data_ptr()), nslice, 1 if accumulate else 0, ctypes.c_void_p(ws.data_ptr()), nbytes,
+              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return C
+
+
+def mp2_transform(eri, Co, Cv, gemm="ozaki", nslice=6):
+    """(ia|jb) from the dense AO tensor by four quarter transforms.
+    gemm="fp64": cuBLAS DGEMM; gemm="ozaki": BF16 tensor cores with FP64 accuracy."""
+    n, o = Co.shape
+    v = Cv.shape[1]
+    if gemm == "fp64":
+        t1 = (Co.T @ eri.reshape(n, n ** 3)).reshape(o, n, n * n)        # (i nu | lam sig)
+        t2 = torch.matmul(Cv.T, t1)                                       # (i a | lam sig)
+        del t1
+        t3 = torch.matmul(Co.T, t2.reshape(o * v, n, n))                  # (i a | j sig)
+        del t2
+        return torch.matmul(t3, Cv).reshape(o, v, o, v)                   # (i a | j b)
+    dev = eri.device
+    E = eri.reshape(-1)
+    Co, Cv = Co.contiguous(), Cv.contiguous()
+    # Y1[i][(b c d)] = sum_a Co[a][i] E[a][(b c d)]
+    Y1 = torch.empty(o * n ** 3, dtype=torch.float64, device=dev)
+    ozaki_gemm(Co, E, Y1, 1, o, n ** 3, n, (0, 1, o), (0, n ** 3, 1), 0, nslice)
+    # Y2[i][a'][(c d)] = sum_b Cv[b][a'] Y1[i][b][(c d)]
+    Y2 = torch.empty(o * v * n * n, dtype=torch.float64, device=dev)
+    ozaki_gemm(Cv, Y1, Y2, o, v, n * n, n, (0, 1, v), (n ** 3, n * n, 1), v * n * n, nslice)
+    del Y1
+    # Y3[(i a)][j][d] = sum_c Co[c][j] Y2[(i a)][c][d]
+    Y3 = torch.empty(o * v * o * n, dtype=torch.float64, device=dev)
+    ozaki_gemm(Co, Y2, Y3, o * v, o, n, n, (0, 1, o), (n * n, n, 1), o * n, nslice)
+    del Y2
+    # T[(i a j)][b] = sum_d Y3[(i a j)][d] Cv[d][b]
+    T = torch.empty(o * v * o * v, dtype=torch.float64, device=dev)
+    ozaki_gemm(Y3, Cv, T, 1, o * v * o, v, n, (0, n, 1), (0, v, 1), 0, nslice)
+    return T.reshape(o, v, o, v)
+
+
+def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6):
     """Closed-shell MP2 correlation energy: four quarter transforms of the dense AO
-    tensor to (ia|jb) (FP64 GEMMs) and the energy denominator sum."""
+    tensor to (ia|jb) and the energy denominator sum."""
     mol = engine.mol
     o = mol.NAlphaElectrons
-    n = engine.nbf
     if eri is None:
         eri = engine.dense_eri()
-    nmo = C.shape[1]
-    v = nmo - o
     Co = C[:, :o].contiguous()
     Cv = C[:, o:].contiguous()
-    t1 = (Co.T @ eri.reshape(n, n ** 3)).reshape(o, n, n * n)            # (i nu | lam sig)
-    t2 = torch.matmul(Cv.T, t1)                                           # (i a | lam sig)
-    del t1
-    t3 = torch.matmul(Co.T, t2.reshape(o * v, n, n))                      # (i a | j sig)
-    del t2
-    ovov = torch.matmul(t3, Cv).reshape(o, v, o, v)                       # (i a | j b)
+    ovov = mp2_transform(eri, Co, Cv, gemm=gemm, nslice=nslice)
     eo, ev = eps[:o], eps[o:]
     den = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
     e2 = torch.sum(ovov * (2.0 * ovov - ovov.permute(0, 3, 2, 1)) / den)
