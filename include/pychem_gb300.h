@@ -214,6 +214,16 @@ size_t pcg_ozaki_workspace(const pcg_gemm_desc_t *desc, int nslice);
 int pcg_ozaki_gemm(const pcg_gemm_desc_t *desc, const double *A, const double *B, double *C, int nslice,
                    int accumulate, void *workspace, size_t ws_bytes, void *stream);
 
+/* Batched symmetric eigensolver (no upstream counterpart; replaces the LAPACK eigh of
+ * Methods/hartree_fock.py:172-175,226): parallel cyclic Jacobi, one CTA per matrix.
+ * A: batch x n x n FP64 (read only); w: batch x n eigenvalues (unsorted, matching the
+ * columns of V); V: batch x m x m with m = n rounded up to even, FP64 (fp32 = 0,
+ * n <= 136) or FP32 (fp32 = 1, n <= 334); V0 (optional, same type/layout as V):
+ * starting rotation, i.e. A is diagonalised as V0 * (V0^T A V0-space) -- pass NULL
+ * for the identity.  info (optional): sweeps used per matrix. */
+int pcg_jacobi_eigh(int batch, int n, const double *A, double *w, void *V, int fp32, const void *V0,
+                    int max_sweeps, double tol, int *info, void *stream);
+
 /* Arithmetic-throughput probe (measurement support, no upstream counterpart): blocks x
  * threads threads each run 8 independent FMA chains of `iters` steps in FP64 (fp32 = 0)
  * or FP32, writing one value per thread to `out` (blocks*threads elements). */

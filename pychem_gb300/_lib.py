@@ -71,6 +71,8 @@ _SIGS = {
                         c_void_p, c_void_p],
     "pcg_fma_probe": [c_int, c_int, c_int, c_int, c_void_p, c_void_p],
     "pcg_ozaki_workspace": [ctypes.c_void_p, c_int],
+    "pcg_jacobi_eigh": [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_double, c_void_p,
+                        c_void_p],
     "pcg_ozaki_gemm": [ctypes.c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, ctypes.c_size_t,
                        c_void_p],
     "pcg_fock_build_noalloc": [ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_int, c_void_p, c_void_p, c_void_p,
@@ -78,7 +80,7 @@ _SIGS = {
 }
 # entry points that launch exactly one kernel of this library per call
 LAUNCHERS = {"pcg_pair_data", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
-             "pcg_digest_class", "pcg_fock_build", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm",
+             "pcg_digest_class", "pcg_fock_build", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh",
              "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",
              "pcg_two_electron_vrr", "pcg_two_electron_contract", "pcg_two_electron_hrr",
              "pcg_one_electron_fundamentals", "pcg_one_electron_vrr", "pcg_one_electron_hrr",

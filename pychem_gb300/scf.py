@@ -19,61 +19,92 @@ MP2 is the closed-shell form of ``Methods/mp2.py:43-94`` (identical value for RH
 import math
 import time
 
+import numpy as np
 import torch
+
+from . import eigen
 
 LINEAR_DEPENDENCE = 1.0e-6   # Data/constants.py:34
 
 
 def orthogonaliser(S):
-    s, U = torch.linalg.eigh(S)
+    s, U = eigen.eigh(S, exact=True)
     s = torch.flip(s, [0])
     U = torch.flip(U, [1])
     keep = s > LINEAR_DEPENDENCE
     return U[:, keep] * s[keep].rsqrt()
 
 
+def diis_coefficients(B):
+    """Pulay C1 coefficients from the (m x m) residual inner-product matrix
+    (``Methods/hf_extensions/diis.py:108-112``), solved on the host (m <= ~16)."""
+    m = B.shape[0]
+    M = -np.ones((m + 1, m + 1))
+    M[:m, :m] = B
+    M[m, m] = 0.0
+    rhs = np.zeros(m + 1)
+    rhs[m] = -1.0
+    return np.linalg.solve(M, rhs)[:m]
+
+
 class SCFResult(dict):
     __getattr__ = dict.get
 
 
-def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=1, D0=None, record=False):
+def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=1, D0=None, record=False,
+        guess="sad"):
     """Restricted Hartree-Fock on a prepared GpuEngine.  Returns SCFResult with
-    E (total), E_elec, C, eps, D (alpha density), iterations, converged, timings."""
+    E (total), E_elec, C, eps, D (alpha density), iterations, converged.
+    guess: "sad" (superposition of atomic densities, default), "core" (upstream's
+    core-Hamiltonian guess), or an explicit alpha density D0."""
     mol = engine.mol
     nocc = mol.NAlphaElectrons
     if mol.NAlphaElectrons != mol.NBetaElectrons:
         raise ValueError("rhf needs a closed-shell molecule")
     S, H = engine.S, engine.H
+    dev = S.device
     e_nuc = mol.nuclear_repulsion()
     X = orthogonaliser(S)
     Xt = X.T.contiguous()
+    state = {"Q": None}
 
-    def diagonalise(F):
-        e, Cp = torch.linalg.eigh(Xt @ F @ X)
-        return e, X @ Cp
+    def diagonalise(F, exact=False):
+        e, Q = eigen.eigh(Xt @ F @ X, X_prev=state["Q"], refine_steps=2, exact=exact, nocc=nocc)
+        state["Q"] = Q
+        return e, X @ Q
 
-    if D0 is None:
+    if D0 is not None:
+        D = D0.clone()
+    elif guess == "sad":
+        from .guess import sad_density
+        D = sad_density(mol, device=dev)
+    else:
         eps, C = diagonalise(H)
         D = C[:, :nocc] @ C[:, :nocc].T
-    else:
-        D = D0.clone()
     n = engine.nbf
-    F = torch.empty(n, n, dtype=torch.float64, device=S.device)
-    G = torch.empty(n, n, dtype=torch.float64, device=S.device)
+    F = torch.empty(n, n, dtype=torch.float64, device=dev)
+    G = torch.empty(n, n, dtype=torch.float64, device=dev)
     focks, resids = [], []
-    E_old = None
+    Bmat = np.zeros((0, 0))
+    E_old = D_old = None
     history = []
     converged = False
     it = 0
-    t_fock = 0.0
     for it in range(1, max_iter + 1):
-        t0 = time.perf_counter()
         engine.fock(D, out=F, G=G)
-        E = float(torch.sum(D * (H + F))) + e_nuc
-        t_fock += time.perf_counter() - t0
-        drms = None
+        use_diis = it > diis_start
+        R = Xt @ (S @ D @ F - F @ D @ S) @ X if use_diis else None
+        # one device->host read per iteration: energy, density change, new DIIS row
+        vals = [torch.sum(D * (H + F)).reshape(1)]
+        vals.append(torch.sqrt(torch.mean((D - D_old) ** 2)).reshape(1) if D_old is not None
+                    else torch.zeros(1, dtype=torch.float64, device=dev))
+        if use_diis:
+            rv = R.reshape(-1)
+            vals.append(torch.stack([torch.dot(rv, r.reshape(-1)) for r in resids] + [torch.dot(rv, rv)]))
+        host = torch.cat(vals).cpu().numpy()
+        E = float(host[0]) + e_nuc
         if E_old is not None:
-            drms = float(torch.sqrt(torch.mean((D - D_old) ** 2)))
+            drms = float(host[1])
             dE = E - E_old
             if record:
                 history.append((it, E, dE, drms))
@@ -81,31 +112,33 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                 converged = True
                 break
         E_old, D_old = E, D
-        R = Xt @ (S @ D @ F - F @ D @ S) @ X
         Fx = F
-        if it > diis_start:
+        if use_diis:
+            row = host[2:]
+            m = len(resids) + 1
+            Bn = np.zeros((m, m))
+            Bn[:m - 1, :m - 1] = Bmat
+            Bn[m - 1, :] = row
+            Bn[:, m - 1] = row
             focks.append(F.clone())
             resids.append(R)
+            Bmat = Bn
             if len(focks) > diis_size:
                 focks.pop(0); resids.pop(0)
-            m = len(focks)
-            if m > 1:
-                Rs = torch.stack([r.reshape(-1) for r in resids])
-                B = torch.empty(m + 1, m + 1, dtype=torch.float64, device=S.device)
-                B[:m, :m] = Rs @ Rs.T
-                B[m, :m] = -1.0
-                B[:m, m] = -1.0
-                B[m, m] = 0.0
-                rhs = torch.zeros(m + 1, dtype=torch.float64, device=S.device)
-                rhs[m] = -1.0
-                c = torch.linalg.solve(B, rhs)[:m]
-                Fx = torch.einsum("k,kij->ij", c, torch.stack(focks))
-        eps, C = diagonalise(Fx)
+                Bmat = Bmat[1:, 1:]
+            if len(focks) > 1:
+                c = diis_coefficients(Bmat)
+                cw = torch.tensor(c, dtype=torch.float64, device=dev)
+                Fx = torch.einsum("k,kij->ij", cw, torch.stack(focks))
+        # first iterations move the orbitals a lot: exact solver; afterwards refine the
+        # previous eigenvectors (checked, with fallback)
+        eps, C = diagonalise(Fx, exact=it <= 3)
         D = C[:, :nocc] @ C[:, :nocc].T
-    # orbitals of the final Fock matrix
-    eps, C = diagonalise(F)
+    # orbitals of the final Fock matrix, exact (including inside near-degenerate
+    # clusters) for MP2's denominators
+    eps, C = diagonalise(F, exact=True)
     return SCFResult(E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=C, eps=eps, D=D, F=F, iterations=it,
-                     converged=converged, history=history, fock_builds=it, t_fock=t_fock)
+                     converged=converged, history=history, fock_builds=it)
 
 
 def ozaki_gemm(A, B, C, batch, M, N, K, sA, sB, sCb, nslice=6, accumulate=False):

@@ -69,6 +69,15 @@ def test_rhf_energy(engines, name):
         assert abs(r.E - float(g["E_rhf"])) < 1e-8
 
 
+@pytest.mark.parametrize("name", ["h2o_631g", "water_dimer_631g"])
+def test_core_and_sad_guess_agree(engines, name):
+    from pychem_gb300.scf import rhf
+    g, eng = engines[name]
+    a, b = rhf(eng, guess="core"), rhf(eng, guess="sad")
+    assert a.converged and b.converged
+    assert abs(a.E - b.E) < 1e-9
+
+
 @pytest.mark.parametrize("name", ["h2o_sto3g", "h2o_631g"])
 def test_mp2_energy(engines, name):
     from pychem_gb300.scf import rhf, rmp2
