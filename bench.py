@@ -208,6 +208,49 @@ def probe_peak(torch, _lib, fp32):
     return best
 
 
+def ensemble_leg(torch, args, n=1024):
+    """1024 perturbed H2O/NH3/CH4/HF/CH3OH/C2H6 (6-31G, 11-30 AO) in one batched SCF,
+    against looping the one-molecule GPU SCF over a sample of the same ensemble."""
+    from pychem_gb300 import workloads as W
+    from pychem_gb300.engine import GpuEngine
+    from pychem_gb300.ensemble import EnsembleEngine, rhf_batched
+    from pychem_gb300.molecule import Molecule
+    from pychem_gb300.scf import rhf
+    mols = [Molecule(c, "6-31G") for c in W.ensemble(n=n, seed=SEED)]
+    eng = EnsembleEngine(mols)
+    times, res = [], None
+    for k in range(args.warmup + max(1, args.steps)):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        eng.compute_pair_data()
+        eng.one_electron(); eng.schwarz(); eng.build_tasks(); eng.compute_eris()
+        res = rhf_batched(eng)
+        e1.record()
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    t_batch = statistics.mean(times)
+    sample = mols[:24]
+    loop_t = []
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E_loop = []
+        for mol in sample:
+            E_loop.append(rhf(GpuEngine(mol).prepare()).E)
+        torch.cuda.synchronize()
+        loop_t.append(time.perf_counter() - t0)
+    per = min(loop_t) / len(sample)
+    dE = max(abs(a - b) for a, b in zip(E_loop, res.E[:len(sample)]))
+    return {"workload": "1024 instances cycling H2O, NH3, CH4, HF, CH3OH, C2H6, 6-31G, N(0, 0.08 A) jitter",
+            "instances": n, "batched_s": t_batch, "instances_per_s": n / t_batch,
+            "looped_instances_per_s": 1.0 / per, "speedup_vs_loop": per * n / t_batch,
+            "converged": int(res.converged.sum()), "max_scf_iterations": int(res.iterations.max()),
+            "quartets": eng.stats["quartets"], "max_dE_vs_loop": dE,
+            "loop_sample": "first %d instances, one GpuEngine + rhf each" % len(sample)}
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -322,6 +365,8 @@ def gpu_arm(args):
     a.record(); rmp2(eng, r.C, r.eps, gemm="fp64"); b.record(); torch.cuda.synchronize()
     t_mp2_fp64 = a.elapsed_time(b) / 1e3
 
+    ens = ensemble_leg(torch, args) if world == 1 or rank == 0 else None
+
     # max over ranks
     if world > 1:
         tt = torch.tensor([t_step, t_e2e], device="cuda")
@@ -368,6 +413,7 @@ def gpu_arm(args):
         "fock_digest": {"s_per_build": t_fock, "store_bytes": store_bytes,
                         "hbm_frac": store_bytes / t_fock / 1e9 / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None},
         "cpu_baseline": cpu,
+        "ensemble": ens,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": out["h2d_bytes"],
                 "d2h_bytes_per_step": out["d2h_bytes"]},
         "gpu_launches": launches,

@@ -129,6 +129,14 @@ typedef struct {
   int nshell, nprim, natom, nbf;
   const int *sh_l, *sh_nprim, *sh_prim, *sh_ao, *sh_atom;
   const double *sh_xyz, *pr_exp, *pr_cc, *at_xyz, *at_z;
+  /* Matrix layout.  One molecule: ld = nbf, sh_blk = sh_at0 = sh_nat = NULL.  An
+   * ensemble of molecules in one set of launches: sh_ao holds AO offsets local to the
+   * shell's molecule, matrix element (p, q) of that molecule lives at
+   * sh_blk[shell] + p * ld + q, and nuclear attraction for the shell runs over atoms
+   * [sh_at0[shell], sh_at0[shell] + sh_nat[shell]). */
+  int ld;
+  const long long *sh_blk;
+  const int *sh_at0, *sh_nat;
 } pcg_basis_t;
 
 /* Shell pairs (A = higher angular momentum) and their primitive-pair data. */
@@ -175,6 +183,8 @@ int pcg_expand_tasks(int nbra, const int *bra, const int *ket, const long long *
 int pcg_digest_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                      int ntask, const double *store, const double *D, double *G, void *stream);
 int pcg_fock_build(int n, const double *H, const double *G, double *F, void *stream);
+/* Same for nblocks consecutive ld x ld blocks (an ensemble of molecules). */
+int pcg_fock_build_batched(int nblocks, int ld, const double *H, const double *G, double *F, void *stream);
 
 /* No counterpart in the upstream code.  The same Fock build as pcg_digest_class over
  * nclass classes followed by pcg_fock_build, for callers that cannot allocate device

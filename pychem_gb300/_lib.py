@@ -25,7 +25,8 @@ class BasisT(ctypes.Structure):
     _fields_ = [("nshell", c_int), ("nprim", c_int), ("natom", c_int), ("nbf", c_int),
                 ("sh_l", c_void_p), ("sh_nprim", c_void_p), ("sh_prim", c_void_p), ("sh_ao", c_void_p),
                 ("sh_atom", c_void_p), ("sh_xyz", c_void_p), ("pr_exp", c_void_p), ("pr_cc", c_void_p),
-                ("at_xyz", c_void_p), ("at_z", c_void_p)]
+                ("at_xyz", c_void_p), ("at_z", c_void_p), ("ld", c_int), ("sh_blk", c_void_p), ("sh_at0", c_void_p),
+                ("sh_nat", c_void_p)]
 
 
 class GemmDescT(ctypes.Structure):
@@ -67,6 +68,7 @@ _SIGS = {
     "pcg_digest_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p,
                          c_void_p, c_void_p, c_void_p],
     "pcg_fock_build": [c_int, c_void_p, c_void_p, c_void_p, c_void_p],
+    "pcg_fock_build_batched": [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
     "pcg_dense_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p,
                         c_void_p, c_void_p],
     "pcg_fma_probe": [c_int, c_int, c_int, c_int, c_void_p, c_void_p],
@@ -80,7 +82,7 @@ _SIGS = {
 }
 # entry points that launch exactly one kernel of this library per call
 LAUNCHERS = {"pcg_pair_data", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
-             "pcg_digest_class", "pcg_fock_build", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh",
+             "pcg_digest_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh",
              "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",
              "pcg_two_electron_vrr", "pcg_two_electron_contract", "pcg_two_electron_hrr",
              "pcg_one_electron_fundamentals", "pcg_one_electron_vrr", "pcg_one_electron_hrr",

@@ -214,9 +214,11 @@ __global__ void k_one_electron(DevBasis b, BoysTable bt, int npair, const int* p
           Tc[ka * ncb + kb] += cc * U * t;
         }
       }
-      // nuclear attraction: Obara-Saika with auxiliary index over all nuclei
+      // nuclear attraction: Obara-Saika with auxiliary index over the molecule's nuclei
       const int L = la + lb;
-      for (int c = 0; c < b.natom; ++c) {
+      const int c0 = b.sh_at0 ? b.sh_at0[A] : 0;
+      const int c1 = b.sh_at0 ? c0 + b.sh_nat[A] : b.natom;
+      for (int c = c0; c < c1; ++c) {
         const double* C = b.at_xyz + 3 * c;
         double PC[3], pc2 = 0.0;
         for (int i = 0; i < 3; ++i) { PC[i] = P[i] - C[i]; pc2 += PC[i] * PC[i]; }
@@ -273,7 +275,10 @@ __global__ void k_one_electron(DevBasis b, BoysTable bt, int npair, const int* p
   // spherical transform and store both triangles
   const int nsa = 2 * la + 1, nsb = 2 * lb + 1;
   const int oa = b.sh_ao[A], ob = b.sh_ao[B];
-  const int n = b.nbf;
+  const int n = b.ld;
+  const long long o = b.sh_blk ? b.sh_blk[A] : 0ll;
+  S += o;
+  H += o;
   for (int r = 0; r < nsa; ++r)
     for (int q = 0; q < nsb; ++q) {
       double s = 0.0, h = 0.0;

@@ -17,6 +17,7 @@ int pcg_launch_schwarz(int cls, const int2* tasks, int ntask, const double* stor
 int pcg_launch_expand(int nbra, const int* bra, const int* ket, const long long* off, const int* qstart,
                       const int* diag, long long ntask, int2* out, cudaStream_t s);
 int pcg_launch_fock(int n, const double* H, const double* G, double* F, cudaStream_t s);
+int pcg_launch_fock_batched(int nblocks, int ld, const double* H, const double* G, double* F, cudaStream_t s);
 
 static DevBasis to_dev(const pcg_basis_t* b) {
   DevBasis d;
@@ -24,6 +25,8 @@ static DevBasis to_dev(const pcg_basis_t* b) {
   d.sh_l = b->sh_l; d.sh_nprim = b->sh_nprim; d.sh_prim = b->sh_prim; d.sh_ao = b->sh_ao;
   d.sh_atom = b->sh_atom; d.sh_xyz = b->sh_xyz; d.pr_exp = b->pr_exp; d.pr_cc = b->pr_cc;
   d.at_xyz = b->at_xyz; d.at_z = b->at_z;
+  d.ld = b->ld > 0 ? b->ld : b->nbf;
+  d.sh_blk = b->sh_blk; d.sh_at0 = b->sh_at0; d.sh_nat = b->sh_nat;
   return d;
 }
 
@@ -104,9 +107,15 @@ int pcg_fock_build(int n, const double* H, const double* G, double* F, void* str
   return pcg_launch_fock(n, H, G, F, (cudaStream_t)stream);
 }
 
+int pcg_fock_build_batched(int nblocks, int ld, const double* H, const double* G, double* F, void* stream) {
+  if (nblocks < 1 || ld < 1) { pcg_set_error("pcg_fock_build_batched: bad arguments"); return PCG_ERR_ARG; }
+  return pcg_launch_fock_batched(nblocks, ld, H, G, F, (cudaStream_t)stream);
+}
+
 int pcg_dense_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
                     const double* store, double* eri, void* stream) {
   if (cls < 0 || cls > 20 || !basis || !pairs) { pcg_set_error("pcg_dense_class: bad arguments"); return PCG_ERR_ARG; }
+  if (basis->sh_blk) { pcg_set_error("pcg_dense_class: one molecule only"); return PCG_ERR_UNSUPPORTED; }
   return pcg_launch_dense(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, eri,
                           (cudaStream_t)stream);
 }

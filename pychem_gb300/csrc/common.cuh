@@ -170,7 +170,18 @@ struct DevBasis {
   const double* pr_cc;
   const double* at_xyz;      // [natom][3]
   const double* at_z;
+  // matrix layout: element (p, q) of the shell's molecule lives at
+  //   blk(shell) + p * ld + q   (p, q local AO indices); a single molecule has
+  //   blk = 0, ld = nbf.  Nuclear attraction runs over the molecule's atoms only.
+  int ld;
+  const long long* sh_blk;   // nullptr: 0 for every shell
+  const int* sh_at0;         // nullptr: atoms [0, natom)
+  const int* sh_nat;
 };
+
+__device__ __forceinline__ long long dev_blk(const DevBasis& b, int sh) {
+  return b.sh_blk ? __ldg(b.sh_blk + sh) : 0ll;
+}
 
 struct DevPairs {
   int npair, npp;

@@ -32,8 +32,11 @@ __global__ void __launch_bounds__(128) k_digest(DevBasis b, DevPairsExt pr, cons
   const int2 tk = tasks[t];
   const int A = __ldg(pr.p.A + tk.x), B = __ldg(pr.p.B + tk.x);
   const int C = __ldg(pr.p.A + tk.y), Dd = __ldg(pr.p.B + tk.y);
+  const long long o = dev_blk(b, A);  // the four shells share one molecule
   const int oa = __ldg(b.sh_ao + A), ob = __ldg(b.sh_ao + B), oc = __ldg(b.sh_ao + C), od = __ldg(b.sh_ao + Dd);
-  const int n = b.nbf;
+  const int n = b.ld;
+  D += o;
+  G += o;
   const double deg = (A == B ? 1.0 : 2.0) * (C == Dd ? 1.0 : 2.0) * (tk.x == tk.y ? 1.0 : 2.0);
   double Dab[NA][NB], Dcd[NC][ND], Dac[NA][NC], Dbd[NB][ND], Dad[NA][ND], Dbc[NB][NC];
   double gab[NA][NB], gcd[NC][ND], gac[NA][NC], gbd[NB][ND], gad[NA][ND], gbc[NB][NC];
@@ -283,6 +286,25 @@ __global__ void k_fock(int n, const double* __restrict__ H, const double* __rest
   if (idx >= n * n) return;
   const int i = idx / n, j = idx % n;
   F[idx] = H[idx] + 0.5 * (G[idx] + G[(size_t)j * n + i]);
+}
+
+// F = H + (G + G^T)/2 for nblocks consecutive ld x ld blocks
+__global__ void k_fock_batched(long long total, int ld, const double* __restrict__ H, const double* __restrict__ G,
+                               double* __restrict__ F) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const long long sq = (long long)ld * ld;
+  const long long base = idx / sq * sq;
+  const int r = (int)(idx - base);
+  const int i = r / ld, j = r % ld;
+  F[idx] = H[idx] + 0.5 * (G[idx] + G[base + (long long)j * ld + i]);
+}
+
+int pcg_launch_fock_batched(int nblocks, int ld, const double* H, const double* G, double* F, cudaStream_t s) {
+  const long long total = (long long)nblocks * ld * ld;
+  k_fock_batched<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(total, ld, H, G, F);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
 }
 
 int pcg_launch_fock(int n, const double* H, const double* G, double* F, cudaStream_t s) {

@@ -35,6 +35,8 @@ static DevBasis basis_of(const pcg_basis_t* b) {
   d.sh_l = b->sh_l; d.sh_nprim = b->sh_nprim; d.sh_prim = b->sh_prim; d.sh_ao = b->sh_ao;
   d.sh_atom = b->sh_atom; d.sh_xyz = b->sh_xyz; d.pr_exp = b->pr_exp; d.pr_cc = b->pr_cc;
   d.at_xyz = b->at_xyz; d.at_z = b->at_z;
+  d.ld = b->ld > 0 ? b->ld : b->nbf;
+  d.sh_blk = b->sh_blk; d.sh_at0 = b->sh_at0; d.sh_nat = b->sh_nat;
   return d;
 }
 
@@ -56,6 +58,10 @@ extern "C" int pcg_fock_build_noalloc(const pcg_basis_t* basis, const pcg_pairs_
     return PCG_ERR_ARG;
   }
   const int n = basis->nbf;
+  if (basis->sh_blk) {
+    pcg_set_error("pcg_fock_build_noalloc: one molecule only");
+    return PCG_ERR_UNSUPPORTED;
+  }
   if (n <= 0 || n > PCG_NOALLOC_MAX_NBF) {
     char msg[160];
     snprintf(msg, sizeof(msg), "pcg_fock_build_noalloc: nbf = %d exceeds the static scratch limit of %d basis functions",

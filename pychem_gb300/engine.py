@@ -67,6 +67,7 @@ class GpuEngine:
         b.nshell = len(a["sh_l"]); b.nprim = len(a["pr_exp"]); b.natom = len(a["at_z"]); b.nbf = self.mol.NOrbitals
         for k in ("sh_l", "sh_nprim", "sh_prim", "sh_ao", "sh_atom", "sh_xyz", "pr_exp", "pr_cc", "at_xyz", "at_z"):
             setattr(b, k, self.d[k].data_ptr())
+        b.ld = self.mol.NOrbitals
         self.basis_t = b
         self.nbf = self.mol.NOrbitals
 
@@ -79,6 +80,10 @@ class GpuEngine:
         swap = lb > la
         A = np.where(swap, ib, ia).astype(np.int32)
         B = np.where(swap, ia, ib).astype(np.int32)
+        self._finish_pairs(A, B)
+
+    def _finish_pairs(self, A, B):
+        a = self.h_basis
         nA, nB = a["sh_nprim"][A], a["sh_nprim"][B]
         npp = (nA * nB).astype(np.int32)
         ppoff = np.concatenate([[0], np.cumsum(npp)[:-1]]).astype(np.int32)
@@ -202,6 +207,11 @@ class GpuEngine:
                 entry["64"].append((kb, kk, n64, np.zeros(len(Qr), dtype=np.int32), diag))
                 if n32.sum() > 0:
                     entry["32"].append((kb, kk, n32, c64.astype(np.int32), np.zeros(len(Qr), dtype=np.int32)))
+        return self._expand(per_class)
+
+    def _expand(self, per_class):
+        """Materialise the per-bra (count, first ket, diagonal) bucket plans as int2
+        task lists on the GPU, one per class and precision."""
         self.classes = {}
         nq64 = nq32 = 0
         for cls, entry in sorted(per_class.items()):

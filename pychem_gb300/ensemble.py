@@ -1,0 +1,298 @@
+"""Batched RHF of an ensemble of small molecules in one set of launches.
+
+Every molecule of the ensemble is a separate RHF problem (the upstream code runs them
+one input section at a time, ``pychem.py:146-160``).  Here all of them share each
+launch: shells of all molecules are concatenated, shell pairs and quartets are built
+only inside a molecule, one-electron integrals see only the molecule's own nuclei, and
+every matrix is a padded ``nbf_max x nbf_max`` block per molecule (padding AOs get
+S = 1 and H = 1e3 on the diagonal, so they only form far-virtual orbitals).  The SCF
+then runs on (batch, nbf_max, nbf_max) tensors: batched Fock digestion, batched FP64
+Jacobi eigensolver (one CTA per molecule), batched DIIS.
+"""
+import ctypes
+import time
+
+import numpy as np
+import torch
+
+from . import _lib, eigen
+from ._lib import BasisT
+from .engine import GpuEngine, _ptr, _stream, pair_class
+from .scf import SCFResult
+
+PAD_DIAG = 1.0e3
+
+
+class EnsembleEngine(GpuEngine):
+    def __init__(self, molecules, device="cuda", precision="fp64", fp32_below=1e-4, threshold=1e-8):
+        self.mols = list(molecules)
+        self.B = len(self.mols)
+        self.nmax = max(m.NOrbitals for m in self.mols)
+        self.mol = self.mols[0]
+        super().__init__(self.mols[0], device=device, precision=precision, fp32_below=fp32_below,
+                         threshold=threshold)
+
+    # ---------------------------------------------------------------------------------
+    def _upload_basis(self):
+        arrs = [m.arrays() for m in self.mols]
+        nsh = [len(a["sh_l"]) for a in arrs]
+        npr = [len(a["pr_exp"]) for a in arrs]
+        nat = [len(a["at_z"]) for a in arrs]
+        sh_off = np.concatenate([[0], np.cumsum(nsh)[:-1]])
+        pr_off = np.concatenate([[0], np.cumsum(npr)[:-1]])
+        at_off = np.concatenate([[0], np.cumsum(nat)[:-1]])
+        n2 = self.nmax * self.nmax
+        a = dict(
+            sh_l=np.concatenate([x["sh_l"] for x in arrs]).astype(np.int32),
+            sh_nprim=np.concatenate([x["sh_nprim"] for x in arrs]).astype(np.int32),
+            sh_prim=np.concatenate([x["sh_prim"] + o for x, o in zip(arrs, pr_off)]).astype(np.int32),
+            sh_ao=np.concatenate([x["sh_ao"] for x in arrs]).astype(np.int32),
+            sh_atom=np.concatenate([x["sh_atom"] + o for x, o in zip(arrs, at_off)]).astype(np.int32),
+            sh_xyz=np.concatenate([x["sh_xyz"] for x in arrs]),
+            pr_exp=np.concatenate([x["pr_exp"] for x in arrs]),
+            pr_cc=np.concatenate([x["pr_cc"] for x in arrs]),
+            at_xyz=np.concatenate([x["at_xyz"] for x in arrs]),
+            at_z=np.concatenate([x["at_z"] for x in arrs]),
+            sh_blk=np.concatenate([np.full(k, m * n2, dtype=np.int64) for m, k in enumerate(nsh)]),
+            sh_at0=np.concatenate([np.full(k, o, dtype=np.int32) for k, o in zip(nsh, at_off)]),
+            sh_nat=np.concatenate([np.full(k, na, dtype=np.int32) for k, na in zip(nsh, nat)]),
+            sh_mol=np.concatenate([np.full(k, m, dtype=np.int32) for m, k in enumerate(nsh)]),
+        )
+        self.sh_off = sh_off
+        self.h_basis = a
+        self.d = {k: self._t(v) for k, v in a.items()}
+        b = BasisT()
+        b.nshell = len(a["sh_l"]); b.nprim = len(a["pr_exp"]); b.natom = len(a["at_z"]); b.nbf = self.nmax
+        for k in ("sh_l", "sh_nprim", "sh_prim", "sh_ao", "sh_atom", "sh_xyz", "pr_exp", "pr_cc", "at_xyz", "at_z",
+                  "sh_blk", "sh_at0", "sh_nat"):
+            setattr(b, k, self.d[k].data_ptr())
+        b.ld = self.nmax
+        self.basis_t = b
+        self.nbf = self.nmax
+
+    def _pair_index(self):
+        """Shell pairs a <= b inside each molecule (global shell indices)."""
+        ia_all, ib_all = [], []
+        for m, mol in enumerate(self.mols):
+            n = mol.NCgtf
+            ia, ib = np.triu_indices(n)
+            ia_all.append(ia + self.sh_off[m])
+            ib_all.append(ib + self.sh_off[m])
+        return np.concatenate(ia_all), np.concatenate(ib_all)
+
+    def _build_pairs(self):
+        a = self.h_basis
+        ia, ib = self._pair_index()
+        la, lb = a["sh_l"][ia], a["sh_l"][ib]
+        swap = lb > la
+        A = np.where(swap, ib, ia).astype(np.int32)
+        B = np.where(swap, ia, ib).astype(np.int32)
+        self._finish_pairs(A, B)
+        self.pair_mol = a["sh_mol"][A]
+
+    # ---------------------------------------------------------------------------------
+    def one_electron(self):
+        n = self.nmax
+        S = torch.zeros(self.B, n, n, dtype=torch.float64, device=self.dev)
+        H = torch.zeros(self.B, n, n, dtype=torch.float64, device=self.dev)
+        _lib.call("pcg_one_electron", ctypes.byref(self.basis_t), self.npair, _ptr(self.pd["A"]), _ptr(self.pd["B"]),
+                  _ptr(S), _ptr(H), _stream())
+        nb = torch.tensor([m.NOrbitals for m in self.mols], device=self.dev)
+        pad = torch.arange(n, device=self.dev).unsqueeze(0) >= nb.unsqueeze(1)           # (B, n)
+        S += torch.diag_embed(pad.to(torch.float64))
+        H += torch.diag_embed(pad.to(torch.float64) * PAD_DIAG)
+        self.S, self.H = S, H
+        return S, H
+
+    def _segments(self, ids):
+        mol = self.pair_mol[ids]
+        starts = np.searchsorted(mol, np.arange(self.B), side="left")
+        ends = np.searchsorted(mol, np.arange(self.B), side="right")
+        return mol, starts, ends
+
+    def build_tasks(self):
+        """As GpuEngine.build_tasks, with every quartet inside one molecule: within a
+        pair kind the pairs are ordered by (molecule, -Q), so the kets of a bra are a
+        prefix of its molecule's segment."""
+        Qh = self.Q.cpu().numpy()
+        thr, thr32 = self.threshold, self.fp32_below
+        kp, ks = [], []
+        for k in range(len(self.kinds)):
+            ids = np.nonzero(self.pair_kind == k)[0]
+            o = np.lexsort((-Qh[ids], self.pair_mol[ids]))
+            kp.append(ids[o].astype(np.int32))
+            ks.append(Qh[ids[o]])
+        self.kind_pairs_dev = [self._t(x) for x in kp]
+        qmax = float(Qh.max()) + 1.0
+        span = 2.0 * qmax + 1.0
+
+        def prefix_count(bra_ids, Qr, ket_ids, Qk, t):
+            kmol, kst, ken = self._segments(ket_ids)
+            bmol = self.pair_mol[bra_ids]
+            key = kmol * span + (qmax - Qk)
+            q = bmol * span + qmax - t / np.maximum(Qr, 1e-300)
+            c = np.searchsorted(key, q, side="left")
+            lo, hi = kst[bmol], ken[bmol]
+            c = np.clip(c, lo, hi)
+            nk = len(Qk)
+            for _ in range(3):   # exact predicate Qr*Qk > t at the boundary
+                up = (c < hi) & (Qr * Qk[np.minimum(c, nk - 1)] > t)
+                c = c + up
+                dn = (c > lo) & ~(Qr * Qk[np.maximum(c - 1, 0)] > t)
+                c = c - dn
+            return (c - lo).astype(np.int64), lo.astype(np.int64)
+
+        per_class = {}
+        nk = len(self.kinds)
+        for kb in range(nk):
+            for kk in range(kb + 1):
+                bra_ids, ket_ids = kp[kb], kp[kk]
+                if len(bra_ids) == 0 or len(ket_ids) == 0:
+                    continue
+                la, lb = int(self.h_pairs["lA"][bra_ids[0]]), int(self.h_pairs["lB"][bra_ids[0]])
+                lc, ld = int(self.h_pairs["lA"][ket_ids[0]]), int(self.h_pairs["lB"][ket_ids[0]])
+                cls = _lib.load().pcg_eri_class_id(la, lb, lc, ld)
+                Qr, Qk = ks[kb], ks[kk]
+                c, seg0 = prefix_count(bra_ids, Qr, ket_ids, Qk, thr)
+                if thr32 > 0:
+                    c32, _ = prefix_count(bra_ids, Qr, ket_ids, Qk, thr32)
+                else:
+                    c32 = c.copy()
+                c32 = np.minimum(c32, c)
+                if kb == kk:
+                    r = np.arange(len(Qr), dtype=np.int64) - seg0
+                    cnt = np.minimum(r + 1, c)
+                    diag = (c <= r).astype(np.int32)
+                    c64 = np.minimum(cnt, c32)
+                else:
+                    cnt = c
+                    diag = np.zeros(len(Qr), dtype=np.int32)
+                    c64 = c32
+                entry = per_class.setdefault(cls, {"64": [], "32": []})
+                entry["64"].append((kb, kk, c64 + diag, seg0.astype(np.int32), diag))
+                if (cnt - c64).sum() > 0:
+                    entry["32"].append((kb, kk, cnt - c64, (seg0 + c64).astype(np.int32),
+                                        np.zeros(len(Qr), dtype=np.int32)))
+        return self._expand(per_class)
+
+    # ---------------------------------------------------------------------------------
+    def fock(self, D, out=None, G=None):
+        n = self.nmax
+        if G is None:
+            G = torch.zeros(self.B, n, n, dtype=torch.float64, device=self.dev)
+        else:
+            G.zero_()
+        D = D.contiguous()
+        for cls, rec in self.classes.items():
+            for part, (tasks, ntask) in rec.items():
+                _lib.call("pcg_digest_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t), _ptr(tasks),
+                          ntask, _ptr(self.stores[(cls, part)]), _ptr(D), _ptr(G), _stream())
+        F = out if out is not None else torch.empty(self.B, n, n, dtype=torch.float64, device=self.dev)
+        _lib.call("pcg_fock_build_batched", self.B, n, _ptr(self.H), _ptr(G), _ptr(F), _stream())
+        return F
+
+    def dense_eri(self):
+        raise NotImplementedError("dense ERI tensors are built per molecule (GpuEngine)")
+
+
+def sad_batch(eng):
+    from .guess import atomic_density
+    n = eng.nmax
+    D = torch.zeros(eng.B, n, n, dtype=torch.float64, device=eng.dev)
+    for m, mol in enumerate(eng.mols):
+        ao = 0
+        for sym, Z, _ in mol.atoms:
+            Da = atomic_density(sym, Z, mol.Basis, eng.dev)
+            k = Da.shape[0]
+            D[m, ao:ao + k, ao:ao + k] = Da
+            ao += k
+    return D
+
+
+def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="sad", D0=None):
+    """RHF of every molecule of a prepared EnsembleEngine.  Returns SCFResult with
+    per-molecule arrays E, iterations (first iteration meeting the criteria), and C,
+    eps (batch, nbf_max, ...)."""
+    B, n, dev = eng.B, eng.nmax, eng.dev
+    S, H = eng.S, eng.H
+    e_nuc = np.array([m.nuclear_repulsion() for m in eng.mols])
+    nocc = torch.tensor([m.NAlphaElectrons for m in eng.mols], device=dev)
+    for m in eng.mols:
+        if m.NAlphaElectrons != m.NBetaElectrons:
+            raise ValueError("rhf_batched needs closed-shell molecules")
+    s, U = eigen.eigh(S)
+    if float(s.min()) <= 1e-6:
+        raise ValueError("linear dependence in an ensemble member; use GpuEngine for it")
+    X = U * s.rsqrt().unsqueeze(-2)
+    Xt = X.transpose(-1, -2).contiguous()
+    occ = (torch.arange(n, device=dev).unsqueeze(0) < nocc.unsqueeze(1)).to(torch.float64)   # (B, n)
+    state = {"Q": None}
+
+    def density(Fx):
+        e, Q = eigen.eigh(Xt @ Fx @ X, X_prev=state["Q"])
+        state["Q"] = Q
+        C = X @ Q
+        return e, C, (C * occ.unsqueeze(-2)) @ C.transpose(-1, -2)
+
+    if D0 is not None:
+        D = D0.clone()
+    elif guess == "sad":
+        D = sad_batch(eng)
+    else:
+        _, _, D = density(H)
+    F = torch.empty_like(S)
+    G = torch.empty_like(S)
+    focks, resids = [], []
+    Bm = np.zeros((B, 0, 0))
+    E_old = None
+    D_old = None
+    done_at = np.zeros(B, dtype=np.int64)
+    E_at = np.zeros(B)
+    it = 0
+    for it in range(1, max_iter + 1):
+        eng.fock(D, out=F, G=G)
+        R = Xt @ (S @ D @ F - F @ D @ S) @ X
+        Rf = R.reshape(B, -1)
+        vals = [torch.sum(D * (H + F), dim=(1, 2))]
+        vals.append(torch.sqrt(torch.mean((D - D_old) ** 2, dim=(1, 2))) if D_old is not None
+                    else torch.zeros(B, dtype=torch.float64, device=dev))
+        vals += [torch.sum(Rf * r.reshape(B, -1), dim=1) for r in resids] + [torch.sum(Rf * Rf, dim=1)]
+        host = torch.stack(vals, dim=1).cpu().numpy()
+        E = host[:, 0] + e_nuc
+        if E_old is not None:
+            ok = (np.abs(E - E_old) < e_tol) & (host[:, 1] < d_tol) & (done_at == 0)
+            done_at[ok] = it
+            E_at[ok] = E[ok]
+            if (done_at > 0).all():
+                break
+        E_old, D_old = E, D
+        row = host[:, 2:]
+        m = row.shape[1]
+        Bn = np.zeros((B, m, m))
+        Bn[:, :m - 1, :m - 1] = Bm
+        Bn[:, m - 1, :] = row
+        Bn[:, :, m - 1] = row
+        focks.append(F.clone())
+        resids.append(R)
+        Bm = Bn
+        if len(focks) > diis_size:
+            focks.pop(0); resids.pop(0)
+            Bm = Bm[:, 1:, 1:]
+        Fx = F
+        k = len(focks)
+        if k > 1:
+            M = -np.ones((B, k + 1, k + 1))
+            M[:, :k, :k] = Bm
+            M[:, k, k] = 0.0
+            rhs = np.zeros((B, k + 1))
+            rhs[:, k] = -1.0
+            c = np.linalg.solve(M, rhs[..., None])[:, :k, 0]
+            cw = torch.tensor(c, dtype=torch.float64, device=dev)
+            Fx = torch.einsum("bk,kbij->bij", cw, torch.stack(focks))
+        eps, C, D = density(Fx)
+    still = done_at == 0
+    E_at[still] = E[still]
+    state["Q"] = None
+    eps, C, _ = density(F)
+    return SCFResult(E=E_at, iterations=np.where(done_at > 0, done_at, it), converged=~still, C=C, eps=eps, D=D,
+                     scf_iterations=it)
