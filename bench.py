@@ -251,6 +251,45 @@ def ensemble_leg(torch, args, n=1024):
             "loop_sample": "first %d instances, one GpuEngine + rhf each" % len(sample)}
 
 
+def alkane_leg(torch, args):
+    """C12H26 / cc-pVDZ (298 AO, s/p/d): plain FP64 vs mixed precision (quartets with
+    Schwarz bound below 1e-4 in FP32, everything else and all accumulation in FP64)."""
+    from pychem_gb300 import workloads as W
+    from pychem_gb300.engine import GpuEngine
+    from pychem_gb300.molecule import Molecule
+    from pychem_gb300.scf import rhf
+    mol = Molecule(W.alkane(12, seed=SEED), "cc-pVDZ")
+    out = {"workload": "C12H26 all-trans, N(0, 0.03 A) jitter, cc-pVDZ, %d AO" % mol.NOrbitals}
+    for prec in ("fp64", "mixed"):
+        eng = GpuEngine(mol, precision=prec, fp32_below=1e-4)
+        ts, te = [], []
+        for k in range(2 + max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record()
+            eng.compute_pair_data(); eng.one_electron(); eng.schwarz(); eng.build_tasks()
+            e1.record()
+            eng.compute_eris()
+            e2.record()
+            r = rhf(eng)
+            torch.cuda.synchronize()
+            if k >= 2:
+                te.append(e1.elapsed_time(e2) / 1e3)
+                ts.append(e0.elapsed_time(e1) / 1e3)
+            t_tot = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.compute_pair_data(); eng.one_electron(); eng.schwarz(); eng.build_tasks(); eng.compute_eris()
+        r = rhf(eng)
+        torch.cuda.synchronize()
+        out[prec] = {"ttc_s": time.perf_counter() - t0, "eri_s": statistics.mean(te), "E_rhf": r.E,
+                     "iterations": r.iterations, "quartets_fp32": eng.stats["quartets_fp32"],
+                     "quartets_fp64": eng.stats["quartets_fp64"]}
+    out["dE_mixed_vs_fp64"] = out["mixed"]["E_rhf"] - out["fp64"]["E_rhf"]
+    out["eri_speedup_mixed"] = out["fp64"]["eri_s"] / out["mixed"]["eri_s"]
+    return out
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -366,6 +405,7 @@ def gpu_arm(args):
     t_mp2_fp64 = a.elapsed_time(b) / 1e3
 
     ens = ensemble_leg(torch, args) if world == 1 or rank == 0 else None
+    alk = alkane_leg(torch, args) if world == 1 or rank == 0 else None
 
     # max over ranks
     if world > 1:
@@ -414,6 +454,7 @@ def gpu_arm(args):
                         "hbm_frac": store_bytes / t_fock / 1e9 / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None},
         "cpu_baseline": cpu,
         "ensemble": ens,
+        "alkane_mixed": alk,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": out["h2d_bytes"],
                 "d2h_bytes_per_step": out["d2h_bytes"]},
         "gpu_launches": launches,

@@ -234,6 +234,23 @@ int pcg_ozaki_gemm(const pcg_gemm_desc_t *desc, const double *A, const double *B
 int pcg_jacobi_eigh(int batch, int n, const double *A, double *w, void *V, int fp32, const void *V0,
                     int max_sweeps, double tol, int *info, void *stream);
 
+/* Learned initial guess (no upstream counterpart; upstream's guesses are the core
+ * Hamiltonian and MO files, Methods/hartree_fock.py:35-57).  Dense-layer kernels:
+ * C[m][n] (+)= sum_k A[m*sam + k*sak] B[k*sbk + n*sbn] with FP32 A, FP32 or BF16 B
+ * (b_bf16), FP32 accumulation, optional epilogue Z = C + bias, C = silu(Z) (act = 1);
+ * G *= silu'(Z); column sums; masked squared error (dY = 2 (Y - T) mask * inv_count,
+ * loss += sum of squares * inv_count); Adam on FP32 master weights with an optional
+ * BF16 copy (bias-corrected by step). */
+int pcg_mlp_gemm(int M, int N, int K, const float *A, long long sam, long long sak, const void *B,
+                 int b_bf16, long long sbk, long long sbn, float *C, int ldc, int accumulate,
+                 const float *bias, float *Z, int act, void *stream);
+int pcg_mlp_dsilu(long long n, float *dY, const float *Z, void *stream);
+int pcg_mlp_colsum(int M, int N, const float *G, float *db, void *stream);
+int pcg_mlp_mse(long long n, const float *Y, const float *T, const float *mask, float inv_count,
+                float *dY, float *loss, void *stream);
+int pcg_mlp_adam(long long n, float *w, const float *g, float *m, float *v, void *w_bf16, float lr,
+                 float b1, float b2, float eps, int step, void *stream);
+
 /* Arithmetic-throughput probe (measurement support, no upstream counterpart): blocks x
  * threads threads each run 8 independent FMA chains of `iters` steps in FP64 (fp32 = 0)
  * or FP32, writing one value per thread to `out` (blocks*threads elements). */

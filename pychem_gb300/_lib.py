@@ -73,6 +73,13 @@ _SIGS = {
                         c_void_p, c_void_p],
     "pcg_fma_probe": [c_int, c_int, c_int, c_int, c_void_p, c_void_p],
     "pcg_ozaki_workspace": [ctypes.c_void_p, c_int],
+    "pcg_mlp_gemm": [c_int, c_int, c_int, c_void_p, c_longlong, c_longlong, c_void_p, c_int, c_longlong, c_longlong,
+                     c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p],
+    "pcg_mlp_dsilu": [c_longlong, c_void_p, c_void_p, c_void_p],
+    "pcg_mlp_colsum": [c_int, c_int, c_void_p, c_void_p, c_void_p],
+    "pcg_mlp_mse": [c_longlong, c_void_p, c_void_p, c_void_p, ctypes.c_float, c_void_p, c_void_p, c_void_p],
+    "pcg_mlp_adam": [c_longlong, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_float, ctypes.c_float,
+                     ctypes.c_float, ctypes.c_float, c_int, c_void_p],
     "pcg_jacobi_eigh": [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_double, c_void_p,
                         c_void_p],
     "pcg_ozaki_gemm": [ctypes.c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, ctypes.c_size_t,
@@ -82,7 +89,8 @@ _SIGS = {
 }
 # entry points that launch exactly one kernel of this library per call
 LAUNCHERS = {"pcg_pair_data", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
-             "pcg_digest_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh",
+             "pcg_digest_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh", "pcg_mlp_gemm", "pcg_mlp_dsilu",
+             "pcg_mlp_colsum", "pcg_mlp_mse", "pcg_mlp_adam",
              "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",
              "pcg_two_electron_vrr", "pcg_two_electron_contract", "pcg_two_electron_hrr",
              "pcg_one_electron_fundamentals", "pcg_one_electron_vrr", "pcg_one_electron_hrr",

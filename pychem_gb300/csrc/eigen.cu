@@ -160,20 +160,27 @@ extern "C" int pcg_jacobi_eigh(int batch, int n, const double* A, double* w, voi
   const int m = n + (n & 1);
   if (m / 2 > 512 || m < 2) { pcg_set_error("pcg_jacobi_eigh: n out of range"); return PCG_ERR_UNSUPPORTED; }
   cudaStream_t s = (cudaStream_t)stream;
+  {
+    const cudaError_t prior = cudaGetLastError();
+    if (prior != cudaSuccess) {
+      pcg_set_cuda_error(prior, "an earlier asynchronous operation (reported on entry to pcg_jacobi_eigh)");
+      return PCG_ERR_CUDA;
+    }
+  }
   const long long sA = (long long)n * n, sV = (long long)m * m, sw = n;
   if (!fp32) {
     const size_t smem = ((size_t)(m * (m + 1) / 2 + 1) / 2 * 2 + (size_t)m * m) * sizeof(double);
     if (smem > 220 * 1024) { pcg_set_error("pcg_jacobi_eigh: FP64 variant needs n <= 136"); return PCG_ERR_UNSUPPORTED; }
     const int threads = m <= 32 ? 128 : 256;
-    if (smem > 48 * 1024)
-      PCG_CUDA(cudaFuncSetAttribute(k_jacobi<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // opt in to the exact dynamic size: dynamic + static (12.5 KB) may exceed the
+    // 48 KB default even when the dynamic part alone does not
+    PCG_CUDA(cudaFuncSetAttribute(k_jacobi<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_jacobi<double, true><<<batch, threads, smem, s>>>(n, m, A, sA, (double*)V, sV, (const double*)V0, w, sw,
                                                          max_sweeps, tol, info);
   } else {
     const size_t smem = (size_t)m * (m + 1) / 2 * sizeof(float);
     if (smem > 220 * 1024) { pcg_set_error("pcg_jacobi_eigh: FP32 variant needs n <= 334"); return PCG_ERR_UNSUPPORTED; }
-    if (smem > 48 * 1024)
-      PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_jacobi<float, false><<<batch, 1024, smem, s>>>(n, m, A, sA, (float*)V, sV, (const float*)V0, w, sw, max_sweeps,
                                                       tol, info);
   }

@@ -222,9 +222,7 @@ extern "C" int pcg_ozaki_gemm(const pcg_gemm_desc_t* d, const double* A, const d
   float* P = (float*)(ws + L.offP);
   // split A: vectors (b, m) along k; B: vectors (b, n) along k
   const size_t smem = (size_t)OZ_VB * d->K * sizeof(double);
-  if (smem > 48 * 1024) {
-    PCG_CUDA(cudaFuncSetAttribute(k_oz_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  }
+  PCG_CUDA(cudaFuncSetAttribute(k_oz_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   {
     const long long nb = d->sAb ? d->batch : 1;
     const long long nv = nb * d->M;

@@ -195,17 +195,36 @@ class EnsembleEngine(GpuEngine):
         raise NotImplementedError("dense ERI tensors are built per molecule (GpuEngine)")
 
 
+def atom_blocks(mols):
+    """Per-atom rows (molecule, first AO, number of AOs, symbol, Z) of an ensemble."""
+    mol_i, ao0, nao, sym, zz = [], [], [], [], []
+    for m, mol in enumerate(mols):
+        ao = 0
+        for (s, Z, _), k in zip(mol.atoms, mol.atom_nao()):
+            mol_i.append(m); ao0.append(ao); nao.append(k); sym.append(s); zz.append(Z)
+            ao += k
+    return np.array(mol_i), np.array(ao0), np.array(nao), sym, zz
+
+
 def sad_batch(eng):
+    """Superposition of free-atom densities for every molecule, (B, nmax, nmax): one
+    scatter per (element, basis) of the ensemble."""
     from .guess import atomic_density
     n = eng.nmax
     D = torch.zeros(eng.B, n, n, dtype=torch.float64, device=eng.dev)
-    for m, mol in enumerate(eng.mols):
-        ao = 0
-        for sym, Z, _ in mol.atoms:
-            Da = atomic_density(sym, Z, mol.Basis, eng.dev)
-            k = Da.shape[0]
-            D[m, ao:ao + k, ao:ao + k] = Da
-            ao += k
+    mol_i, ao0, nao, sym, zz = atom_blocks(eng.mols)
+    bas = [eng.mols[m].Basis for m in mol_i]
+    groups = {}
+    for k, key in enumerate(zip(sym, bas)):
+        groups.setdefault(key, []).append(k)
+    for (s, b), rows in groups.items():
+        rows = np.array(rows)
+        Da = atomic_density(s, zz[rows[0]], b, eng.dev)
+        k = Da.shape[0]
+        r = torch.arange(k, device=eng.dev)
+        m = torch.as_tensor(mol_i[rows], device=eng.dev)[:, None, None]
+        a = torch.as_tensor(ao0[rows], device=eng.dev)[:, None, None]
+        D[m, a + r[:, None], a + r[None, :]] = Da.unsqueeze(0).expand(len(rows), k, k)
     return D
 
 

@@ -98,6 +98,13 @@ class Molecule:
                     sh_xyz=np.ascontiguousarray(sh_xyz), pr_exp=pr_exp, pr_cc=pr_cc,
                     at_xyz=np.ascontiguousarray(at_xyz), at_z=at_z)
 
+    def atom_nao(self):
+        """Number of AOs of each atom (an atom's AOs are contiguous)."""
+        n = [0] * self.NAtom
+        for l, _, _, ia in self.shells:
+            n[ia] += 2 * l + 1
+        return n
+
     def nuclear_repulsion(self):
         """Methods/integrals.py:196-207."""
         e = 0.0

@@ -12,7 +12,7 @@ def rand_sym(batch, n, seed, spread=1.0):
     return A * spread
 
 
-@pytest.mark.parametrize("n", [1, 2, 7, 13, 30, 64, 101])
+@pytest.mark.parametrize("n", [1, 2, 7, 13, 30, 57, 58, 64, 101, 136])
 def test_fp64_jacobi_batched(n):
     from pychem_gb300 import eigen
     A = rand_sym(17, n, n)
