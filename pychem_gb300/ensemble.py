@@ -18,7 +18,7 @@ import torch
 from . import _lib, eigen
 from ._lib import BasisT
 from .engine import GpuEngine, _ptr, _stream, pair_class
-from .scf import SCFResult
+from .scf import SCFResult, diis_coefficients_batched
 
 PAD_DIAG = 1.0e3
 
@@ -69,6 +69,39 @@ class EnsembleEngine(GpuEngine):
         b.ld = self.nmax
         self.basis_t = b
         self.nbf = self.nmax
+
+    def atom_table(self):
+        if getattr(self, "_atoms", None) is None:
+            self._atoms = atom_table(self.mols)
+        return self._atoms
+
+    def restrict(self, active):
+        """Cut the quartet lists and integral stores down to the molecules with
+        active[m] (host bool array); unrestrict() brings back the full ones."""
+        if getattr(self, "_full", None) is None:
+            self._full = (self.classes, self.stores)
+        if getattr(self, "_pair_mol_dev", None) is None:
+            self._pair_mol_dev = torch.as_tensor(self.pair_mol, dtype=torch.int64, device=self.dev)
+        on = torch.as_tensor(active, device=self.dev)
+        classes, stores = {}, {}
+        for cls, rec in self.classes.items():
+            nout = _lib.load().pcg_eri_class_nout(cls)
+            new = {}
+            for part, (tasks, nt) in rec.items():
+                tv = tasks.view(nt, 2)
+                keep = on[self._pair_mol_dev[tv[:, 0].long()]].nonzero().squeeze(1)
+                if keep.numel() == 0:
+                    continue
+                new[part] = (tv.index_select(0, keep).reshape(-1), keep.numel())
+                stores[(cls, part)] = self.stores[(cls, part)].view(nout, nt).index_select(1, keep).reshape(-1)
+            if new:
+                classes[cls] = new
+        self.classes, self.stores = classes, stores
+
+    def unrestrict(self):
+        if getattr(self, "_full", None) is not None:
+            self.classes, self.stores = self._full
+            self._full = None
 
     def _pair_index(self):
         """Shell pairs a <= b inside each molecule (global shell indices)."""
@@ -195,15 +228,20 @@ class EnsembleEngine(GpuEngine):
         raise NotImplementedError("dense ERI tensors are built per molecule (GpuEngine)")
 
 
-def atom_blocks(mols):
-    """Per-atom rows (molecule, first AO, number of AOs, symbol, Z) of an ensemble."""
-    mol_i, ao0, nao, sym, zz = [], [], [], [], []
-    for m, mol in enumerate(mols):
-        ao = 0
-        for (s, Z, _), k in zip(mol.atoms, mol.atom_nao()):
-            mol_i.append(m); ao0.append(ao); nao.append(k); sym.append(s); zz.append(Z)
-            ao += k
-    return np.array(mol_i), np.array(ao0), np.array(nao), sym, zz
+def atom_table(mols):
+    """Per-atom rows of an ensemble, molecule by molecule: molecule index, first AO
+    inside the molecule, AO count, Z, symbol, position (bohr); plus per molecule the
+    index of its first atom and its atom count."""
+    nat = np.array([m.NAtom for m in mols], dtype=np.int64)
+    mol = np.repeat(np.arange(len(mols)), nat)
+    sym = [a[0] for m in mols for a in m.atoms]
+    z = np.array([a[1] for m in mols for a in m.atoms])
+    xyz = np.array([a[2] for m in mols for a in m.atoms], dtype=np.float64).reshape(-1, 3)
+    nao = np.array([k for m in mols for k in m.atom_nao()], dtype=np.int64)
+    atom0 = np.concatenate([[0], np.cumsum(nat)[:-1]]).astype(np.int64)
+    ao_glob = np.cumsum(nao) - nao
+    ao0 = ao_glob - ao_glob[atom0][mol]
+    return dict(mol=mol, ao0=ao0, nao=nao, z=z, sym=sym, xyz=xyz, atom0=atom0, nat=nat)
 
 
 def sad_batch(eng):
@@ -212,26 +250,32 @@ def sad_batch(eng):
     from .guess import atomic_density
     n = eng.nmax
     D = torch.zeros(eng.B, n, n, dtype=torch.float64, device=eng.dev)
-    mol_i, ao0, nao, sym, zz = atom_blocks(eng.mols)
-    bas = [eng.mols[m].Basis for m in mol_i]
+    at = eng.atom_table()
+    bas = np.array([m.Basis for m in eng.mols])[at["mol"]]
     groups = {}
-    for k, key in enumerate(zip(sym, bas)):
+    for k, key in enumerate(zip(at["sym"], bas)):
         groups.setdefault(key, []).append(k)
     for (s, b), rows in groups.items():
         rows = np.array(rows)
-        Da = atomic_density(s, zz[rows[0]], b, eng.dev)
+        Da = atomic_density(s, at["z"][rows[0]], b, eng.dev)
         k = Da.shape[0]
         r = torch.arange(k, device=eng.dev)
-        m = torch.as_tensor(mol_i[rows], device=eng.dev)[:, None, None]
-        a = torch.as_tensor(ao0[rows], device=eng.dev)[:, None, None]
+        m = torch.as_tensor(at["mol"][rows], device=eng.dev)[:, None, None]
+        a = torch.as_tensor(at["ao0"][rows], device=eng.dev)[:, None, None]
         D[m, a + r[:, None], a + r[None, :]] = Da.unsqueeze(0).expand(len(rows), k, k)
     return D
 
 
-def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="sad", D0=None):
+def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="sad", D0=None, compact=0.5):
     """RHF of every molecule of a prepared EnsembleEngine.  Returns SCFResult with
     per-molecule arrays E, iterations (first iteration meeting the criteria), and C,
-    eps (batch, nbf_max, ...)."""
+    eps, D (batch, nbf_max, ...).
+
+    Molecules leave the iteration when they converge: the dense per-molecule work
+    (commutators, DIIS, eigensolver) runs on the still-active rows only, and once the
+    active molecules are at most `compact` of those the quartet lists cover, the lists
+    and integral stores are cut down to the active molecules (the engine's full lists
+    are restored on return)."""
     B, n, dev = eng.B, eng.nmax, eng.dev
     S, H = eng.S, eng.H
     e_nuc = np.array([m.nuclear_repulsion() for m in eng.mols])
@@ -245,73 +289,102 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
     X = U * s.rsqrt().unsqueeze(-2)
     Xt = X.transpose(-1, -2).contiguous()
     occ = (torch.arange(n, device=dev).unsqueeze(0) < nocc.unsqueeze(1)).to(torch.float64)   # (B, n)
-    state = {"Q": None}
-
-    def density(Fx):
-        e, Q = eigen.eigh(Xt @ Fx @ X, X_prev=state["Q"])
-        state["Q"] = Q
-        C = X @ Q
-        return e, C, (C * occ.unsqueeze(-2)) @ C.transpose(-1, -2)
 
     if D0 is not None:
         D = D0.clone()
     elif guess == "sad":
         D = sad_batch(eng)
     else:
-        _, _, D = density(H)
-    F = torch.empty_like(S)
-    G = torch.empty_like(S)
+        _, Q0 = eigen.eigh(Xt @ H @ X)
+        C0 = X @ Q0
+        D = (C0 * occ.unsqueeze(-2)) @ C0.transpose(-1, -2)
+    # active rows: molecule ids `act` and their slices of every per-molecule tensor
+    act = np.arange(B)
+    Xa, Xta, Sa, Ha, occa, enuc_a = X, Xt, S, H, occ, e_nuc
+    Q = None
+    Dfull = torch.empty_like(S)
+    Ffull = torch.empty_like(S)
+    Gfull = torch.empty_like(S)
+    F_fin = torch.empty_like(S)
+    D_fin = torch.empty_like(S)
     focks, resids = [], []
     Bm = np.zeros((B, 0, 0))
-    E_old = None
-    D_old = None
+    E_old = D_old = None
     done_at = np.zeros(B, dtype=np.int64)
     E_at = np.zeros(B)
+    covered = B
     it = 0
-    for it in range(1, max_iter + 1):
-        eng.fock(D, out=F, G=G)
-        R = Xt @ (S @ D @ F - F @ D @ S) @ X
-        Rf = R.reshape(B, -1)
-        vals = [torch.sum(D * (H + F), dim=(1, 2))]
-        vals.append(torch.sqrt(torch.mean((D - D_old) ** 2, dim=(1, 2))) if D_old is not None
-                    else torch.zeros(B, dtype=torch.float64, device=dev))
-        vals += [torch.sum(Rf * r.reshape(B, -1), dim=1) for r in resids] + [torch.sum(Rf * Rf, dim=1)]
-        host = torch.stack(vals, dim=1).cpu().numpy()
-        E = host[:, 0] + e_nuc
-        if E_old is not None:
-            ok = (np.abs(E - E_old) < e_tol) & (host[:, 1] < d_tol) & (done_at == 0)
-            done_at[ok] = it
-            E_at[ok] = E[ok]
-            if (done_at > 0).all():
-                break
-        E_old, D_old = E, D
-        row = host[:, 2:]
-        m = row.shape[1]
-        Bn = np.zeros((B, m, m))
-        Bn[:, :m - 1, :m - 1] = Bm
-        Bn[:, m - 1, :] = row
-        Bn[:, :, m - 1] = row
-        focks.append(F.clone())
-        resids.append(R)
-        Bm = Bn
-        if len(focks) > diis_size:
-            focks.pop(0); resids.pop(0)
-            Bm = Bm[:, 1:, 1:]
-        Fx = F
-        k = len(focks)
-        if k > 1:
-            M = -np.ones((B, k + 1, k + 1))
-            M[:, :k, :k] = Bm
-            M[:, k, k] = 0.0
-            rhs = np.zeros((B, k + 1))
-            rhs[:, k] = -1.0
-            c = np.linalg.solve(M, rhs[..., None])[:, :k, 0]
-            cw = torch.tensor(c, dtype=torch.float64, device=dev)
-            Fx = torch.einsum("bk,kbij->bij", cw, torch.stack(focks))
-        eps, C, D = density(Fx)
+    try:
+        for it in range(1, max_iter + 1):
+            act_t = torch.as_tensor(act, device=dev)
+            Dfull.index_copy_(0, act_t, D)
+            eng.fock(Dfull, out=Ffull, G=Gfull)
+            F = Ffull.index_select(0, act_t)
+            R = Xta @ (Sa @ D @ F - F @ D @ Sa) @ Xa
+            Rf = R.reshape(len(act), -1)
+            vals = [torch.sum(D * (Ha + F), dim=(1, 2))]
+            vals.append(torch.sqrt(torch.mean((D - D_old) ** 2, dim=(1, 2))) if D_old is not None
+                        else torch.zeros(len(act), dtype=torch.float64, device=dev))
+            vals += [torch.sum(Rf * r.reshape(len(act), -1), dim=1) for r in resids] + [torch.sum(Rf * Rf, dim=1)]
+            host = torch.stack(vals, dim=1).cpu().numpy()
+            E = host[:, 0] + enuc_a
+            if E_old is not None:
+                conv = (np.abs(E - E_old) < e_tol) & (host[:, 1] < d_tol)
+                if conv.any():
+                    ids = act[conv]
+                    ct = torch.as_tensor(np.nonzero(conv)[0], device=dev)
+                    it_ids = torch.as_tensor(ids, device=dev)
+                    done_at[ids] = it
+                    E_at[ids] = E[conv]
+                    F_fin.index_copy_(0, it_ids, F.index_select(0, ct))
+                    D_fin.index_copy_(0, it_ids, D.index_select(0, ct))
+                    if conv.all():
+                        act = act[:0]
+                        break
+                    keep = ~conv
+                    kt = torch.as_tensor(np.nonzero(keep)[0], device=dev)
+                    act = act[keep]
+                    D, F, R = D[kt], F[kt], R[kt]
+                    Xa, Xta, Sa, Ha, occa = Xa[kt], Xta[kt], Sa[kt], Ha[kt], occa[kt]
+                    enuc_a, E, host = enuc_a[keep], E[keep], host[keep]
+                    Q = Q[kt] if Q is not None else None
+                    focks = [f[kt] for f in focks]
+                    resids = [r[kt] for r in resids]
+                    Bm = Bm[keep]
+                    if len(act) <= compact * covered:
+                        mask = np.zeros(B, dtype=bool)
+                        mask[act] = True
+                        eng.restrict(mask)
+                        covered = len(act)
+            E_old, D_old = E, D
+            row = host[:, 2:]
+            m = row.shape[1]
+            Bn = np.zeros((len(act), m, m))
+            Bn[:, :m - 1, :m - 1] = Bm
+            Bn[:, m - 1, :] = row
+            Bn[:, :, m - 1] = row
+            focks.append(F)
+            resids.append(R)
+            Bm = Bn
+            if len(focks) > diis_size:
+                focks.pop(0); resids.pop(0)
+                Bm = Bm[:, 1:, 1:]
+            Fx = F
+            k = len(focks)
+            if k > 1:
+                cw = torch.tensor(diis_coefficients_batched(Bm), dtype=torch.float64, device=dev)
+                Fx = torch.einsum("bk,kbij->bij", cw, torch.stack(focks))
+            _, Q = eigen.eigh(Xta @ Fx @ Xa, X_prev=Q)
+            C = Xa @ Q
+            D = (C * occa.unsqueeze(-2)) @ C.transpose(-1, -2)
+    finally:
+        eng.unrestrict()
+    if len(act):
+        at = torch.as_tensor(act, device=dev)
+        E_at[act] = E
+        F_fin.index_copy_(0, at, F)
+        D_fin.index_copy_(0, at, D)
     still = done_at == 0
-    E_at[still] = E[still]
-    state["Q"] = None
-    eps, C, _ = density(F)
-    return SCFResult(E=E_at, iterations=np.where(done_at > 0, done_at, it), converged=~still, C=C, eps=eps, D=D,
-                     scf_iterations=it)
+    eps, Qf = eigen.eigh(Xt @ F_fin @ X)
+    return SCFResult(E=E_at, iterations=np.where(done_at > 0, done_at, it), converged=~still, C=X @ Qf, eps=eps,
+                     D=D_fin, scf_iterations=it)

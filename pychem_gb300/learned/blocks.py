@@ -63,6 +63,7 @@ def slots(ti, tj):
     return out
 
 
+# the order gives the pair-type index tc = 2 [i is H] + [j is H]
 TYPES = {("X", "X"): slots("X", "X"), ("X", "H"): slots("X", "H"), ("H", "X"): slots("H", "X"),
          ("H", "H"): slots("H", "H")}
 
@@ -203,75 +204,53 @@ def blocks_from_params(par, R, ti, tj):
     return _Tmat(R, ti).transpose(1, 2) @ loc @ _Tmat(R, tj)
 
 
-def pair_list(mols):
-    """All ordered pairs (i, j), i != j, within the cutoff, grouped by pair type and
-    ordered by molecule.  Returns dict type -> arrays (mol, i, j, gi = index of atom i
-    in the ensemble's atom list, ao_i, ao_j, ei, ej, r [A], vec = R_j - R_i [bohr])."""
-    B = len(mols)
-    amax = max(m.NAtom for m in mols)
-    xyz = np.zeros((B, amax, 3))
-    valid = np.zeros((B, amax), dtype=bool)
-    eidx = np.zeros((B, amax), dtype=np.int64)
-    ao = np.zeros((B, amax), dtype=np.int64)
-    nat = np.zeros(B, dtype=np.int64)
-    for m, mol in enumerate(mols):
-        n = mol.NAtom
-        nat[m] = n
-        xyz[m, :n] = [a[2] for a in mol.atoms]
-        valid[m, :n] = True
-        eidx[m, :n] = [EIDX[a[0]] for a in mol.atoms]
-        nao = np.where(eidx[m, :n] == 0, 2, 9)
-        ao[m, 1:n] = np.cumsum(nao)[:-1]
-    atom0 = np.concatenate([[0], np.cumsum(nat)[:-1]])
+ZIDX = torch.full((10,), -1, dtype=torch.int64)
+ZIDX[1], ZIDX[6], ZIDX[7], ZIDX[8] = 0, 1, 2, 3
+
+
+def pairs(at, device):
+    """All ordered atom pairs (i, j), i != j, within the cutoff, from an atom table
+    (mol, ao0, z, xyz [bohr], atom0, nat per molecule), built with tensor operations on
+    `device`, ordered by molecule.  Returns tensors mol, gi, gj (atoms' table rows),
+    ao_i, ao_j, ei, ej (element indices), r [A], vec = R_j - R_i [bohr] and tc, the
+    pair type's index in TYPES."""
+    nat = torch.as_tensor(at["nat"], device=device)
+    nb, amax = nat.numel(), int(nat.max())
+    mol = torch.as_tensor(at["mol"], device=device)
+    N = mol.numel()
+    z = torch.as_tensor(np.rint(at["z"]).astype(np.int64), device=device)
+    if int(z.max()) >= ZIDX.numel() or bool((ZIDX.to(device)[z] < 0).any()):
+        raise ValueError("the learned guess covers H, C, N and O only")
+    eidx = ZIDX.to(device)[z]
+    ao0 = torch.as_tensor(at["ao0"], device=device)
+    loc = torch.arange(N, device=device) - torch.as_tensor(at["atom0"], device=device)[mol]
+    idx = torch.full((nb, amax), -1, dtype=torch.int64, device=device)
+    idx[mol, loc] = torch.arange(N, device=device)
+    xyz = torch.zeros(nb, amax, 3, dtype=torch.float64, device=device)
+    xyz[mol, loc] = torch.as_tensor(at["xyz"], dtype=torch.float64, device=device)
     vec = xyz[:, None, :, :] - xyz[:, :, None, :]
-    r = np.linalg.norm(vec, axis=-1) / TO_BOHR
-    keep = valid[:, :, None] & valid[:, None, :] & ~np.eye(amax, dtype=bool)[None] & (r <= CUTOFF)
-    M, I, J = np.nonzero(keep)
-    isH_i, isH_j = eidx[M, I] == 0, eidx[M, J] == 0
-    out = {}
-    for ti in (False, True):
-        for tj in (False, True):
-            sel = (isH_i == ti) & (isH_j == tj)
-            if not sel.any():
-                continue
-            m, i, j = M[sel], I[sel], J[sel]
-            out[("H" if ti else "X", "H" if tj else "X")] = dict(
-                mol=m, i=i, j=j, gi=atom0[m] + i, ao_i=ao[m, i], ao_j=ao[m, j], ei=eidx[m, i], ej=eidx[m, j],
-                r=r[m, i, j], vec=vec[m, i, j])
-    return out
-
-
-def atom_list(mols):
-    """Per-atom (mol, ao0, is_H) of an ensemble, in the order pair_list's gi counts."""
-    mol_i, ao0, isH = [], [], []
-    for m, mol in enumerate(mols):
-        ao = 0
-        for sym, _, _ in mol.atoms:
-            mol_i.append(m); ao0.append(ao); isH.append(sym == "H")
-            ao += nao_of(sym)
-    return dict(mol=np.array(mol_i, dtype=np.int64), ao0=np.array(ao0, dtype=np.int64), isH=np.array(isH))
+    r = torch.linalg.vector_norm(vec, dim=-1) / TO_BOHR
+    valid = idx >= 0
+    eye = torch.eye(amax, dtype=torch.bool, device=device)
+    keep = valid[:, :, None] & valid[:, None, :] & ~eye[None] & (r <= CUTOFF)
+    m, i, j = keep.nonzero(as_tuple=True)
+    gi, gj = idx[m, i], idx[m, j]
+    ei, ej = eidx[gi], eidx[gj]
+    tc = 2 * (ei == 0).to(torch.int64) + (ej == 0).to(torch.int64)
+    return dict(mol=m, gi=gi, gj=gj, ao_i=ao0[gi], ao_j=ao0[gj], ei=ei, ej=ej, r=r[m, i, j], vec=vec[m, i, j], tc=tc)
 
 
 def features(pl, device):
     ei = torch.as_tensor(pl["ei"], device=device)
     ej = torch.as_tensor(pl["ej"], device=device)
     r = torch.as_tensor(pl["r"], dtype=torch.float32, device=device)
-    P = len(pl["r"])
+    P = r.numel()
     X = torch.zeros(P, NFEAT, dtype=torch.float32, device=device)
     X[torch.arange(P, device=device), ei] = 1.0
     X[torch.arange(P, device=device), 4 + ej] = 1.0
     mu = torch.as_tensor(MU, dtype=torch.float32, device=device)
     X[:, 8:] = torch.exp(-((r.unsqueeze(1) - mu) ** 2) / (2.0 * WIDTH ** 2))
     return X
-
-
-def scatter_diag(D, pl, ti, blk):
-    ni = blk.shape[1]
-    dev = D.device
-    m = torch.as_tensor(pl["mol"], device=dev)[:, None, None].expand(-1, ni, ni)
-    ai = (torch.as_tensor(pl["ao_i"], device=dev)[:, None, None] + torch.arange(ni, device=dev)[None, :, None]).expand(-1, ni, ni)
-    aj = (torch.as_tensor(pl["ao_i"], device=dev)[:, None, None] + torch.arange(ni, device=dev)[None, None, :]).expand(-1, ni, ni)
-    D.index_put_((m, ai, aj), blk, accumulate=True)
 
 
 def gather_blocks(D, pl, t):
@@ -281,14 +260,3 @@ def gather_blocks(D, pl, t):
     ai = torch.as_tensor(pl["ao_i"], device=dev)[:, None, None] + torch.arange(ni, device=dev)[None, :, None]
     aj = torch.as_tensor(pl["ao_j"], device=dev)[:, None, None] + torch.arange(nj, device=dev)[None, None, :]
     return D[m, ai, aj]
-
-
-def scatter_blocks(D, pl, t, blk):
-    ni, nj = blk.shape[1], blk.shape[2]
-    dev = D.device
-    w = 0.5
-    m = torch.as_tensor(pl["mol"], device=dev)[:, None, None].expand(-1, ni, nj)
-    ai = (torch.as_tensor(pl["ao_i"], device=dev)[:, None, None] + torch.arange(ni, device=dev)[None, :, None]).expand(-1, ni, nj)
-    aj = (torch.as_tensor(pl["ao_j"], device=dev)[:, None, None] + torch.arange(nj, device=dev)[None, None, :]).expand(-1, ni, nj)
-    D.index_put_((m, ai, aj), w * blk, accumulate=True)
-    D.index_put_((m, aj, ai), w * blk, accumulate=True)

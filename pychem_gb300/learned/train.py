@@ -57,55 +57,50 @@ def solve(mols, D0=None, guess="sad"):
 TYPE_LIST = list(B.TYPES)
 
 
-def _pairs_cat(pl, device):
-    """Concatenate the pair types of a pair list, ordered by molecule."""
-    keys = [t for t in TYPE_LIST if t in pl]
-    cat = {k: np.concatenate([pl[t][k] for t in keys]) for k in ("mol", "gi", "ao_i", "ao_j", "ei", "ej", "r", "vec")}
-    cat["tc"] = np.concatenate([np.full(len(pl[t]["r"]), TYPE_LIST.index(t)) for t in keys])
-    order = np.argsort(cat["mol"], kind="stable")
-    return {k: v[order] for k, v in cat.items()}
+def _block_index(mol, r0, c0, ni, nj, n):
+    """Flat indices into a (B, n, n) tensor of the (ni x nj) blocks at (r0, c0)."""
+    dev = mol.device
+    ri = torch.arange(ni, device=dev)[None, :, None]
+    cj = torch.arange(nj, device=dev)[None, None, :]
+    return ((mol[:, None, None] * n + r0[:, None, None] + ri) * n + c0[:, None, None] + cj).reshape(-1)
 
 
 def assemble(D, pc, par):
     """Add predicted blocks to D (B, n, n): off-diagonal slots averaged over the two
-    orders of a pair, diagonal corrections summed over neighbours."""
-    dev = D.device
-    tc = torch.as_tensor(pc["tc"], device=dev)
-    R = B.frames(torch.as_tensor(pc["vec"], dtype=torch.float64, device=dev))
-    mol = torch.as_tensor(pc["mol"], device=dev)
-    aoi = torch.as_tensor(pc["ao_i"], device=dev)
-    aoj = torch.as_tensor(pc["ao_j"], device=dev)
+    orders of a pair, diagonal corrections summed over neighbours (atomic adds)."""
+    n = D.shape[-1]
+    flat = D.view(-1)
+    R = B.frames(pc["vec"].to(torch.float64))
     par = par.to(torch.float64)
     for c, (ti, tj) in enumerate(TYPE_LIST):
-        sel = (tc == c).nonzero().squeeze(1)
+        sel = (pc["tc"] == c).nonzero().squeeze(1)
         if sel.numel() == 0:
             continue
         ni, nj = B.nao_of(ti), B.nao_of(tj)
-        ri = torch.arange(ni, device=dev)
-        rj = torch.arange(nj, device=dev)
-        m = mol[sel][:, None, None].expand(-1, ni, nj)
-        ai = (aoi[sel][:, None, None] + ri[None, :, None]).expand(-1, ni, nj)
-        aj = (aoj[sel][:, None, None] + rj[None, None, :]).expand(-1, ni, nj)
+        m, ai, aj = pc["mol"][sel], pc["ao_i"][sel], pc["ao_j"][sel]
         blk = 0.5 * B.blocks_from_params(par[sel, :B.NOFF], R[sel], ti, tj)
-        D.index_put_((m, ai, aj), blk, accumulate=True)
-        D.index_put_((m, aj, ai), blk, accumulate=True)
+        flat.index_add_(0, _block_index(m, ai, aj, ni, nj, n), blk.reshape(-1))
+        flat.index_add_(0, _block_index(m, aj, ai, nj, ni, n), blk.transpose(1, 2).reshape(-1))
         dg = B.diag_from_params(par[sel, B.NOFF:], R[sel], ti)
-        m2 = mol[sel][:, None, None].expand(-1, ni, ni)
-        a1 = (aoi[sel][:, None, None] + ri[None, :, None]).expand(-1, ni, ni)
-        a2 = (aoi[sel][:, None, None] + ri[None, None, :]).expand(-1, ni, ni)
-        D.index_put_((m2, a1, a2), dg, accumulate=True)
+        flat.index_add_(0, _block_index(m, ai, ai, ni, ni, n), dg.reshape(-1))
     return D
 
 
 def guess_density(net, mols, eng=None, device="cuda"):
-    """SAD plus the network's pair blocks and diagonal corrections, (B, nmax, nmax)."""
+    """SAD plus the network's pair blocks and diagonal corrections, (B, nmax, nmax),
+    scaled to the electron count when the engine's overlap is available."""
     if eng is None:
         eng = EnsembleEngine(mols)
     D = sad_batch(eng)
-    pc = _pairs_cat(B.pair_list(mols), device)
-    X = B.features(pc, device)
-    par = net.predict(X)
-    return assemble(D, pc, par)
+    pc = B.pairs(eng.atom_table(), D.device)
+    par = net.predict(B.features(pc, D.device))
+    D = assemble(D, pc, par)
+    # rescale to the molecule's electron count: tr(D S) = N_alpha
+    S = getattr(eng, "S", None)
+    if S is not None:
+        ne = torch.tensor([m.NAlphaElectrons for m in mols], dtype=torch.float64, device=D.device)
+        D *= (ne / torch.einsum("bij,bji->b", D, S))[:, None, None]
+    return D
 
 
 def build_dataset(mols_all, chunks, device="cuda", seed=0):
@@ -113,21 +108,21 @@ def build_dataset(mols_all, chunks, device="cuda", seed=0):
     of the converged diagonal block from the free-atom block) of every converged
     molecule, molecules in a seeded random order so that contiguous ranges are batches."""
     P, A = [], []
-    nmol = 0
+    nmol = natom = 0
     for idx in chunks:
         mols = [mols_all[i] for i in idx]
         eng, res = solve(mols)
         Dc = res.D
-        Ds = sad_batch(eng)
-        pc = _pairs_cat(B.pair_list(mols), device)
-        at = B.atom_list(mols)
-        conv = res.converged
-        # converged diagonal blocks minus the free-atom blocks, 9x9 padded
         dev = Dc.device
+        Ds = sad_batch(eng)
+        at = eng.atom_table()
+        pc = B.pairs(at, dev)
+        conv = torch.as_tensor(res.converged, device=dev)
+        # converged diagonal blocks minus the free-atom blocks, 9x9 padded
         r9 = torch.arange(9, device=dev)
         am = torch.as_tensor(at["mol"], device=dev)[:, None, None]
         a0 = torch.as_tensor(at["ao0"], device=dev)[:, None, None]
-        isH = torch.as_tensor(at["isH"], device=dev)
+        isH = torch.as_tensor(at["z"] == 1.0, device=dev)
         lim = torch.where(isH, 2, 9)[:, None, None]
         ii = (a0 + r9[None, :, None]).clamp_max(Dc.shape[1] - 1)
         jj = (a0 + r9[None, None, :]).clamp_max(Dc.shape[1] - 1)
@@ -135,46 +130,43 @@ def build_dataset(mols_all, chunks, device="cuda", seed=0):
         dD = torch.where(valid, Dc[am, ii, jj] - Ds[am, ii, jj], 0.0).to(torch.float32)
         # off-diagonal targets
         tc = pc["tc"]
-        T = torch.zeros(len(tc), B.NOFF, dtype=torch.float64, device=dev)
-        Mk = torch.zeros(len(tc), B.NOFF, dtype=torch.float32, device=dev)
-        R = B.frames(torch.as_tensor(pc["vec"], dtype=torch.float64, device=dev))
+        T = torch.zeros(tc.numel(), B.NOFF, dtype=torch.float64, device=dev)
+        Mk = torch.zeros(tc.numel(), B.NOFF, dtype=torch.float32, device=dev)
+        R = B.frames(pc["vec"])
         for c, t in enumerate(TYPE_LIST):
-            sel = np.nonzero(tc == c)[0]
-            if len(sel) == 0:
+            sel = (tc == c).nonzero().squeeze(1)
+            if sel.numel() == 0:
                 continue
-            p = {k: pc[k][sel] for k in ("mol", "ao_i", "ao_j")}
-            blk = B.gather_blocks(Dc, p, t)
+            blk = B.gather_blocks(Dc, {k: pc[k][sel] for k in ("mol", "ao_i", "ao_j")}, t)
             par, mask = B.params_from_blocks(blk, R[sel], *t)
-            st = torch.as_tensor(sel, device=dev)
-            T[st] = par
-            Mk[st] = mask.to(torch.float32)
-        keep_p = conv[pc["mol"]]
-        keep_a = conv[at["mol"]]
-        # renumber molecules of this chunk (converged ones only) globally
-        newid = np.cumsum(conv) - 1 + nmol
-        aidx = np.cumsum(keep_a) - 1 + sum(len(x["isH"]) for x in A)
-        kp = torch.as_tensor(np.nonzero(keep_p)[0], device=dev)
-        ka = torch.as_tensor(np.nonzero(keep_a)[0], device=dev)
-        P.append(dict(X=B.features({k: v[keep_p] for k, v in pc.items()}, device), T=T[kp].to(torch.float32),
-                      M=Mk[kp], R=R[kp].to(torch.float32), tc=torch.as_tensor(tc[keep_p], device=dev),
-                      gi=torch.as_tensor(aidx[pc["gi"][keep_p]], device=dev),
-                      mol=newid[pc["mol"][keep_p]]))
-        A.append(dict(dD=dD[ka], isH=isH[ka], mol=newid[at["mol"][keep_a]]))
+            T[sel] = par
+            Mk[sel] = mask.to(torch.float32)
+        kp = conv[pc["mol"]].nonzero().squeeze(1)
+        ka = conv[am[:, 0, 0]].nonzero().squeeze(1)
+        # molecules (converged ones) and atoms renumbered over all chunks
+        newid = torch.cumsum(conv.to(torch.int64), 0) - 1 + nmol
+        aidx = torch.cumsum(conv[am[:, 0, 0]].to(torch.int64), 0) - 1 + natom
+        P.append(dict(X=B.features({k: v[kp] for k, v in pc.items()}, dev), T=T[kp].to(torch.float32), M=Mk[kp],
+                      R=R[kp].to(torch.float32), tc=tc[kp], gi=aidx[pc["gi"][kp]], mol=newid[pc["mol"][kp]]))
+        A.append(dict(dD=dD[ka], isH=isH[ka], mol=newid[am[ka, 0, 0]]))
         nmol += int(conv.sum())
+        natom += ka.numel()
         del eng, res, Dc, Ds
         torch.cuda.empty_cache()
-    pairs = {k: (torch.cat([x[k] for x in P]) if k != "mol" else np.concatenate([x[k] for x in P])) for k in P[0]}
-    atoms = {k: (torch.cat([x[k] for x in A]) if k != "mol" else np.concatenate([x[k] for x in A])) for k in A[0]}
+    pairs = {k: torch.cat([x[k] for x in P]) for k in P[0]}
+    atoms = {k: torch.cat([x[k] for x in A]) for k in A[0]}
     # seeded random molecule order; atoms and pairs re-sorted to it
-    perm = np.random.default_rng(seed).permutation(nmol)
-    ao = np.argsort(perm[atoms["mol"]], kind="stable")
-    inv = np.empty_like(ao)
-    inv[ao] = np.arange(len(ao))
-    po = np.argsort(perm[pairs["mol"]], kind="stable")
     dev = pairs["X"].device
-    pairs = {k: (v[torch.as_tensor(po, device=dev)] if k != "mol" else perm[v[po]]) for k, v in pairs.items()}
-    pairs["gi"] = torch.as_tensor(inv, device=dev)[pairs["gi"]]
-    atoms = {k: (v[torch.as_tensor(ao, device=dev)] if k != "mol" else perm[v[ao]]) for k, v in atoms.items()}
+    perm = torch.as_tensor(np.random.default_rng(seed).permutation(nmol), device=dev)
+    ao = torch.argsort(perm[atoms["mol"]], stable=True)
+    inv = torch.empty_like(ao)
+    inv[ao] = torch.arange(ao.numel(), device=dev)
+    po = torch.argsort(perm[pairs["mol"]], stable=True)
+    pairs = {k: v[po] for k, v in pairs.items()}
+    pairs["gi"] = inv[pairs["gi"]]
+    pairs["mol"] = perm[pairs["mol"]].cpu().numpy()
+    atoms = {k: v[ao] for k, v in atoms.items()}
+    atoms["mol"] = perm[atoms["mol"]].cpu().numpy()
     return pairs, atoms, nmol
 
 
@@ -260,6 +252,11 @@ def evaluate(net, test_mols, chunks):
         r_nn = rhf_batched(eng, D0=D0)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
+        Ds = sad_batch(eng)
+        for key, G in (("sad_err", Ds), ("learned_err", D0)):
+            out.setdefault(key, []).extend(torch.sqrt(torch.mean((G - r_sad.D) ** 2, dim=(1, 2))).tolist())
+        ne = torch.tensor([m.NElectrons for m in mols], dtype=torch.float64, device=D0.device)
+        out.setdefault("learned_dN", []).extend((2.0 * torch.einsum("bij,bji->b", D0, eng.S) - ne).tolist())
         bad = ~r_nn.converged
         out["fallbacks"] += int(bad.sum())
         E_nn = np.where(bad, r_sad.E, r_nn.E)
@@ -296,6 +293,9 @@ def main():
            "mean_iterations_learned": float(np.mean(ev["learned_iterations"])),
            "time_sad_s": ev["sad_s"], "time_learned_s": ev["learned_s"],
            "max_abs_dE": float(np.max(np.abs(ev["dE"]))), "fallbacks": ev["fallbacks"],
+           "rms_density_error_sad": float(np.mean(ev["sad_err"])),
+           "rms_density_error_learned": float(np.mean(ev["learned_err"])),
+           "mean_abs_electron_count_error_learned": float(np.mean(np.abs(ev["learned_dN"]))),
            "wall_s": time.time() - t_start}
     log(json.dumps(rep))
     net.save(args.out)

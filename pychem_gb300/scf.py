@@ -38,13 +38,32 @@ def orthogonaliser(S):
 def diis_coefficients(B):
     """Pulay C1 coefficients from the (m x m) residual inner-product matrix
     (``Methods/hf_extensions/diis.py:108-112``), solved on the host (m <= ~16)."""
-    m = B.shape[0]
-    M = -np.ones((m + 1, m + 1))
-    M[:m, :m] = B
-    M[m, m] = 0.0
-    rhs = np.zeros(m + 1)
-    rhs[m] = -1.0
-    return np.linalg.solve(M, rhs)[:m]
+    return diis_coefficients_batched(np.asarray(B)[None])[0]
+
+
+def diis_coefficients_batched(Bm):
+    """diis_coefficients for a stack (batch, m, m).  Each B is scaled by its largest
+    diagonal entry (the coefficients do not change); a system that is still singular
+    (residuals that vanished or repeat once an SCF has converged) takes the
+    least-squares solution."""
+    nb, m, _ = Bm.shape
+    scale = np.abs(np.diagonal(Bm, axis1=1, axis2=2)).max(axis=1)
+    scale = np.where(scale > 0, scale, 1.0)
+    M = -np.ones((nb, m + 1, m + 1))
+    M[:, :m, :m] = Bm / scale[:, None, None]
+    M[:, m, m] = 0.0
+    rhs = np.zeros((nb, m + 1))
+    rhs[:, m] = -1.0
+    try:
+        return np.linalg.solve(M, rhs[..., None])[:, :m, 0]
+    except np.linalg.LinAlgError:
+        out = np.empty((nb, m))
+        for b in range(nb):
+            try:
+                out[b] = np.linalg.solve(M[b], rhs[b])[:m]
+            except np.linalg.LinAlgError:
+                out[b] = np.linalg.lstsq(M[b], rhs[b], rcond=None)[0][:m]
+        return out
 
 
 class SCFResult(dict):

@@ -53,3 +53,19 @@ def test_one_member_against_oracle(ensemble):
     S, H = b.one_electron()
     ref = O.rhf(S, H, b.eri_dense(), mol.NAlphaElectrons, b.nuclear_repulsion())
     assert abs(res.E[m] - ref["E"]) < 1e-8
+
+
+def test_compaction_changes_nothing(ensemble):
+    """Cutting the quartet lists down to the active molecules (here after every
+    convergence) gives the same energies and iteration counts as never cutting them,
+    and the engine's full lists come back afterwards."""
+    from pychem_gb300.ensemble import rhf_batched
+    mols, eng, res = ensemble
+    n_before = sum(n for rec in eng.classes.values() for (_, n) in rec.values())
+    r_never = rhf_batched(eng, compact=0.0)
+    r_always = rhf_batched(eng, compact=1.0)
+    assert sum(n for rec in eng.classes.values() for (_, n) in rec.values()) == n_before
+    assert (r_never.iterations == r_always.iterations).all()
+    assert np.abs(r_never.E - r_always.E).max() < 1e-12
+    assert np.abs(r_never.E - res.E).max() < 1e-12
+    assert (r_always.D - r_never.D).abs().max().item() < 1e-10

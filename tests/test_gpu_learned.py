@@ -60,7 +60,7 @@ def test_learned_guess_gain_and_energy():
     from pychem_gb300.learned.train import guess_density
     from pychem_gb300.molecule import Molecule
     net = PairMLP.load(WEIGHTS)
-    mols = [Molecule(c, "6-31G") for c in molecules(64, seed=2)]
+    mols = [Molecule(c, "6-31G") for c in molecules(128, seed=2)]
     eng = EnsembleEngine(mols).prepare()
     r_sad = rhf_batched(eng, guess="sad")
     r_nn = rhf_batched(eng, D0=guess_density(net, mols, eng))

@@ -7,7 +7,8 @@ torch = pytest.importorskip("torch")
 
 from pychem_gb300.learned import blocks as B
 from pychem_gb300.learned.molgen import molecules
-from pychem_gb300.learned.train import TYPE_LIST, _pairs_cat, assemble
+from pychem_gb300.ensemble import atom_table
+from pychem_gb300.learned.train import TYPE_LIST, assemble
 from pychem_gb300.molecule import Molecule
 
 
@@ -45,16 +46,20 @@ def test_diagonal_corrections_symmetric_and_covariant(ti):
     assert torch.allclose(blk_r, TQ @ blk @ TQ.transpose(1, 2), atol=1e-12)
 
 
-def test_pair_list_matches_brute_force():
+def test_pairs_match_brute_force():
     mols = _mols(8)
-    pl = B.pair_list(mols)
+    at = atom_table(mols)
+    pc = B.pairs(at, "cpu")
     got = set()
-    for t, p in pl.items():
-        for m, i, j, r in zip(p["mol"], p["i"], p["j"], p["r"]):
-            got.add((int(m), int(i), int(j)))
-            ti = "H" if mols[m].atoms[i][0] == "H" else "X"
-            tj = "H" if mols[m].atoms[j][0] == "H" else "X"
-            assert (ti, tj) == t
+    for k in range(pc["mol"].numel()):
+        m, gi, gj = int(pc["mol"][k]), int(pc["gi"][k]), int(pc["gj"][k])
+        i, j = gi - at["atom0"][m], gj - at["atom0"][m]
+        got.add((m, i, j))
+        ti = "H" if mols[m].atoms[i][0] == "H" else "X"
+        tj = "H" if mols[m].atoms[j][0] == "H" else "X"
+        assert TYPE_LIST[int(pc["tc"][k])] == (ti, tj)
+        assert int(pc["ao_i"][k]) == sum(B.nao_of(a[0]) for a in mols[m].atoms[:i])
+        assert abs(float(pc["r"][k]) - np.linalg.norm(mols[m].atoms[j][2] - mols[m].atoms[i][2]) / B.TO_BOHR) < 1e-12
     want = set()
     for m, mol in enumerate(mols):
         for i, a in enumerate(mol.atoms):
@@ -62,9 +67,7 @@ def test_pair_list_matches_brute_force():
                 if i != j and np.linalg.norm(a[2] - b[2]) / B.TO_BOHR <= B.CUTOFF:
                     want.add((m, i, j))
     assert got == want
-    at = B.atom_list(mols)
-    for p in pl.values():
-        assert (at["mol"][p["gi"]] == p["mol"]).all() and (at["ao0"][p["gi"]] == p["ao_i"]).all()
+    assert (np.diff(pc["mol"].numpy()) >= 0).all()
 
 
 def test_assemble_reproduces_representable_blocks():
@@ -73,10 +76,10 @@ def test_assemble_reproduces_representable_blocks():
     corrections of all neighbours are summed into the atom's own block."""
     mols = _mols(5, seed=4)
     n = max(m.NOrbitals for m in mols)
-    pc = _pairs_cat(B.pair_list(mols), "cpu")
-    P = len(pc["r"])
+    pc = B.pairs(atom_table(mols), "cpu")
+    P = pc["r"].numel()
     g = torch.Generator().manual_seed(5)
-    R = B.frames(torch.as_tensor(pc["vec"], dtype=torch.float64))
+    R = B.frames(pc["vec"])
     D_true = torch.zeros(len(mols), n, n, dtype=torch.float64)
     par = torch.zeros(P, B.NPARAM, dtype=torch.float64)
     for k in range(P):
