@@ -173,7 +173,9 @@ int pcg_eri_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, c
 int pcg_schwarz_class(int cls, const int *tasks, int ntask, const double *store, double *Q,
                       void *stream);
 
-/* Expand one bucket of screened quartets into task pairs (see eri.cu k_expand). */
+/* Expand screened quartet rows into task pairs: row r pairs bra pair bra[r] with the
+ * kets ket[qstart[r] + q] for q < off[r+1] - off[r] - diag[r], and with itself last
+ * when diag[r]; its tasks are written at [off[r], off[r+1]) of out_tasks (int2). */
 int pcg_expand_tasks(int nbra, const int *bra, const int *ket, const long long *off,
                      const int *qstart, const int *diag, long long ntask, int *out_tasks,
                      void *stream);

@@ -46,8 +46,11 @@ __global__ void k_jacobi(int n, int m, const double* __restrict__ Ain, long long
   T* A = (T*)smem_raw;
   const int ntri = m * (m + 1) / 2;
   T* V = V_SMEM ? A + ((ntri + 1) & ~1) : Vg + (size_t)blockIdx.x * sV;
-  __shared__ T cs[512], sn[512];
-  __shared__ int pp[512], qq[512];
+  // rotation tables: m/2 entries (m <= 136 for the shared-memory variant, whose
+  // dynamic part then leaves room for only a few KB of static shared memory)
+  constexpr int HMAX = V_SMEM ? 128 : 512;
+  __shared__ T cs[HMAX], sn[HMAX];
+  __shared__ int pp[HMAX], qq[HMAX];
   __shared__ double red0[32], red1[32];
   __shared__ int stop;
   const int b = blockIdx.x;
@@ -170,9 +173,12 @@ extern "C" int pcg_jacobi_eigh(int batch, int n, const double* A, double* w, voi
   const long long sA = (long long)n * n, sV = (long long)m * m, sw = n;
   if (!fp32) {
     const size_t smem = ((size_t)(m * (m + 1) / 2 + 1) / 2 * 2 + (size_t)m * m) * sizeof(double);
-    if (smem > 220 * 1024) { pcg_set_error("pcg_jacobi_eigh: FP64 variant needs n <= 136"); return PCG_ERR_UNSUPPORTED; }
+    if (smem > 220 * 1024 || m / 2 > 128) {
+      pcg_set_error("pcg_jacobi_eigh: FP64 variant needs n <= 136");
+      return PCG_ERR_UNSUPPORTED;
+    }
     const int threads = m <= 32 ? 128 : 256;
-    // opt in to the exact dynamic size: dynamic + static (12.5 KB) may exceed the
+    // opt in to the exact dynamic size: dynamic + static (3.5 KB) may exceed the
     // 48 KB default even when the dynamic part alone does not
     PCG_CUDA(cudaFuncSetAttribute(k_jacobi<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_jacobi<double, true><<<batch, threads, smem, s>>>(n, m, A, sA, (double*)V, sV, (const double*)V0, w, sw,

@@ -247,9 +247,10 @@ int pcg_launch_schwarz(int cls, const int2* tasks, int ntask, const double* stor
 }
 
 // ----------------------------------------------------------------------------------
-// Task expansion for one bucket: bra r (sorted by Schwarz factor, descending) pairs
-// with ket positions [qstart[r], qstart[r] + cnt[r] - diag[r]) of the ket list, plus
-// its own pair when diag[r] (the diagonal quartet upstream always computes).
+// Task expansion: row r pairs bra pair bra[r] with the kets at positions
+// [qstart[r], qstart[r] + cnt[r] - diag[r]) of the ket list, plus the bra's own pair
+// when diag[r] (the diagonal quartet upstream always computes); cnt[r] = off[r+1] -
+// off[r].
 // ----------------------------------------------------------------------------------
 __global__ void k_expand(int nbra, const int* __restrict__ bra, const int* __restrict__ ket,
                          const long long* __restrict__ off, const int* __restrict__ qstart,
@@ -265,7 +266,7 @@ __global__ void k_expand(int nbra, const int* __restrict__ bra, const int* __res
   const long long q = t - off[r];
   const long long cnt = off[r + 1] - off[r];
   int kp;
-  if (diag[r] && q == cnt - 1) kp = ket[r];
+  if (diag[r] && q == cnt - 1) kp = bra[r];
   else kp = ket[qstart[r] + q];
   out[t] = make_int2(bra[r], kp);
 }

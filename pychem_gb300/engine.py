@@ -32,6 +32,77 @@ def pair_class(la, lb):
     return la * (la + 1) // 2 + lb
 
 
+def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32):
+    """Screened canonical quartet plan (Methods/hartree_fock.py:241-312: the quartet
+    loop, the Schwarz test Q_ab Q_cd > threshold, and the diagonal quartet that is
+    always computed), with tensor operations on Q's device.
+
+    Q, kind, mol: per shell pair its Schwarz factor, kind index (kinds ordered by
+    (pair class, nA, nB)) and molecule; class_table[kb, kc] the ERI class of bra kind
+    kb with ket kind kc <= kb.  Pairs are sorted by (kind, molecule, -Q); for a bra
+    pair and a ket kind the kets of the bra's molecule are one segment of that order
+    and the screened kets a prefix of it, whose length is found by bisection on the
+    exact predicate.  Each quartet is listed once: bra kind >= ket kind, and within
+    one kind the ket comes no later than the bra in the order, the bra's own diagonal
+    quartet always included.  Quartets with Q_ab Q_cd <= thr32 (mixed precision, not
+    the appended diagonal) form the FP32 part.
+
+    Returns ([(class, part, bra pair, off, qstart, diag), ...], ket_list): rows of a
+    class and part ordered by (bra kind, ket kind, bra position) -- buckets of uniform
+    primitive counts -- with bra pair ids, task offsets off (int64, rows + 1, starting
+    at 0), first ket position qstart in ket_list (the pair ids in sorted order) and
+    the diagonal flag; row r covers tasks [off[r], off[r+1])."""
+    dev = Q.device
+    nk = int(class_table.shape[0])
+    o = torch.sort(-Q, stable=True).indices
+    o = o[torch.sort(mol[o], stable=True).indices]
+    o = o[torch.sort(kind[o], stable=True).indices]
+    Qs, ks, ms = Q[o], kind[o], mol[o]
+    seg_key = ks * nmol + ms
+    npair = o.numel()
+    # rows: (position of the bra in the order, ket kind <= bra kind)
+    pos = torch.repeat_interleave(torch.arange(npair, device=dev), ks + 1)
+    first = torch.cumsum(ks + 1, 0) - (ks + 1)
+    kk = torch.arange(pos.numel(), device=dev) - first[pos]
+    kb = ks[pos]
+    ro = torch.sort((kb * nk + kk) * npair + pos).indices
+    pos, kk, kb = pos[ro], kk[ro], kb[ro]
+    qb = Qs[pos]
+    key = kk * nmol + ms[pos]
+    lo = torch.searchsorted(seg_key, key, right=False)
+    hi = torch.searchsorted(seg_key, key, right=True)
+    nbits = int((hi - lo).max()).bit_length() + 1 if pos.numel() else 0
+
+    def prefix(t):
+        # largest c in [0, hi - lo] with qb * Qs[lo + c - 1] > t (Qs descending in a segment)
+        a = torch.zeros_like(lo)
+        b = hi - lo
+        for _ in range(nbits):
+            mid = (a + b + 1) // 2
+            ok = (mid > 0) & (qb * Qs[(lo + mid - 1).clamp(0, max(npair - 1, 0))] > t)
+            a = torch.where(ok, mid, a)
+            b = torch.where(ok, b, mid - 1)
+        return a
+
+    c = prefix(thr)
+    c32 = torch.minimum(prefix(thr32), c) if thr32 > 0 else c
+    same = kk == kb
+    r = pos - lo
+    cnt = torch.where(same, torch.minimum(r + 1, c), c)
+    diag = (same & (c <= r)).to(torch.int64)
+    c64 = torch.minimum(cnt, c32)
+    cls_row = class_table[kb, kk]
+    bra = o[pos]
+    plan = []
+    for part, n, qs, dg in (("64", c64 + diag, lo, diag), ("32", cnt - c64, lo + c64, torch.zeros_like(diag))):
+        live = n > 0
+        for cls in torch.unique(cls_row[live]).tolist():
+            sel = ((cls_row == cls) & live).nonzero().squeeze(1)
+            off = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), torch.cumsum(n[sel], 0)])
+            plan.append((int(cls), part, bra[sel], off, qs[sel], dg[sel]))
+    return plan, o
+
+
 class GpuEngine:
     """Integrals of one molecule on one GPU.
 
@@ -108,11 +179,12 @@ class GpuEngine:
         self.pairs_t = t
         # pair kinds ordered by (pair class, nA, nB)
         keys = np.stack([pair_class(self.h_pairs["lA"], self.h_pairs["lB"]), nA, nB], axis=1)
-        uniq = np.unique(keys, axis=0)
+        uniq, inv = np.unique(keys, axis=0, return_inverse=True)
         order = np.lexsort((uniq[:, 2], uniq[:, 1], uniq[:, 0]))
+        rank = np.empty(len(order), dtype=np.int64)
+        rank[order] = np.arange(len(order))
         self.kinds = [tuple(int(x) for x in uniq[i]) for i in order]
-        kind_index = {k: i for i, k in enumerate(self.kinds)}
-        self.pair_kind = np.array([kind_index[tuple(int(x) for x in r)] for r in keys], dtype=np.int32)
+        self.pair_kind = rank[np.asarray(inv).ravel()].astype(np.int32)
         self.compute_pair_data()
 
     def compute_pair_data(self):
@@ -154,89 +226,45 @@ class GpuEngine:
         return Q
 
     # ---------------------------------------------------------------------------------
+    def _pair_molecule(self):
+        """Molecule index of every shell pair (device int64) and the molecule count."""
+        return torch.zeros(self.npair, dtype=torch.int64, device=self.dev), 1
+
     def build_tasks(self):
-        """Screened canonical quartet lists per class (FP64 part and FP32 part)."""
-        Qh = self.Q.cpu().numpy()
-        thr, thr32 = self.threshold, self.fp32_below
-        kp, ks = [], []   # per kind: pair ids sorted by Q desc, their Q
-        for k in range(len(self.kinds)):
-            ids = np.nonzero(self.pair_kind == k)[0]
-            o = np.argsort(-Qh[ids], kind="stable")
-            kp.append(ids[o].astype(np.int32))
-            ks.append(Qh[ids[o]])
-        self.kind_pairs_dev = [self._t(x) for x in kp]
-
-        def prefix_count(Qr, Qk, t):
-            # number of leading kets with Qr * Qk > t (Qk sorted descending)
-            c = np.searchsorted(-Qk, -(t / np.maximum(Qr, 1e-300)), side="left")
-            n = len(Qk)
-            for _ in range(2):
-                up = (c < n) & (Qr * Qk[np.minimum(c, n - 1)] > t)
-                c = c + up
-                dn = (c > 0) & ~(Qr * Qk[np.maximum(c - 1, 0)] > t)
-                c = c - dn
-            return c.astype(np.int64)
-
-        per_class = {}
+        """Screened canonical quartet lists per class and precision part, planned on the
+        GPU by plan_quartets() and expanded by the library (one launch per class and
+        part)."""
+        dev = self.dev
         nk = len(self.kinds)
-        for kb in range(nk):
-            for kk in range(kb + 1):
-                pb, lab, lbb = self.kinds[kb][0], None, None
-                bra_ids, ket_ids = kp[kb], kp[kk]
-                if len(bra_ids) == 0 or len(ket_ids) == 0:
-                    continue
-                la, lb = int(self.h_pairs["lA"][bra_ids[0]]), int(self.h_pairs["lB"][bra_ids[0]])
-                lc, ld = int(self.h_pairs["lA"][ket_ids[0]]), int(self.h_pairs["lB"][ket_ids[0]])
-                cls = _lib.load().pcg_eri_class_id(la, lb, lc, ld)
-                Qr, Qk = ks[kb], ks[kk]
-                c = prefix_count(Qr, Qk, thr)
-                c32 = prefix_count(Qr, Qk, thr32) if thr32 > 0 else np.full(len(Qr), len(Qk), dtype=np.int64)
-                c32 = np.minimum(c32, c)
-                if kb == kk:
-                    r = np.arange(len(Qr), dtype=np.int64)
-                    cnt = np.minimum(r + 1, c)
-                    diag = (c <= r).astype(np.int32)
-                    c64 = np.minimum(cnt, c32)
-                else:
-                    cnt = c
-                    diag = np.zeros(len(Qr), dtype=np.int32)
-                    c64 = c32
-                n64 = c64 + diag
-                n32 = cnt - c64
-                entry = per_class.setdefault(cls, {"64": [], "32": []})
-                entry["64"].append((kb, kk, n64, np.zeros(len(Qr), dtype=np.int32), diag))
-                if n32.sum() > 0:
-                    entry["32"].append((kb, kk, n32, c64.astype(np.int32), np.zeros(len(Qr), dtype=np.int32)))
-        return self._expand(per_class)
-
-    def _expand(self, per_class):
-        """Materialise the per-bra (count, first ket, diagonal) bucket plans as int2
-        task lists on the GPU, one per class and precision."""
+        order = np.argsort(self.pair_kind, kind="stable")
+        first = order[np.searchsorted(self.pair_kind[order], np.arange(nk))]
+        kl = np.stack([self.h_pairs["lA"][first], self.h_pairs["lB"][first]], axis=1)
+        ct = np.full((nk, nk), -1, dtype=np.int64)
+        lib = _lib.load()
+        for i in range(nk):
+            for j in range(i + 1):
+                ct[i, j] = lib.pcg_eri_class_id(int(kl[i, 0]), int(kl[i, 1]), int(kl[j, 0]), int(kl[j, 1]))
+        mol, nmol = self._pair_molecule()
+        plan, ket_list = plan_quartets(self.Q, torch.as_tensor(self.pair_kind, dtype=torch.int64, device=dev), mol,
+                                       nmol, torch.as_tensor(ct, device=dev), float(self.threshold),
+                                       float(self.fp32_below))
+        totals = torch.stack([x[3][-1] for x in plan]).cpu().tolist() if plan else []
+        ket32 = ket_list.to(torch.int32)
         self.classes = {}
-        nq64 = nq32 = 0
-        for cls, entry in sorted(per_class.items()):
-            rec = {}
-            for part in ("64", "32"):
-                buckets = entry[part]
-                total = int(sum(int(b[2].sum()) for b in buckets))
-                if total == 0:
-                    continue
-                tasks = torch.empty(total * 2, dtype=torch.int32, device=self.dev)
-                pos = 0
-                for (kb, kk, cnt, qstart, diag) in buckets:
-                    ntask = int(cnt.sum())
-                    if ntask == 0:
-                        continue
-                    off = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
-                    d_off, d_qs, d_dg = self._t(off), self._t(qstart), self._t(diag)
-                    sub = tasks[2 * pos:]
-                    _lib.call("pcg_expand_tasks", len(cnt), _ptr(self.kind_pairs_dev[kb]), _ptr(self.kind_pairs_dev[kk]),
-                              _ptr(d_off), _ptr(d_qs), _ptr(d_dg), ntask, _ptr(sub), _stream())
-                    pos += ntask
-                rec[part] = (tasks, total)
-            self.classes[cls] = rec
-            nq64 += rec.get("64", (None, 0))[1]
-            nq32 += rec.get("32", (None, 0))[1]
+        for (cls, part, bra, off, qs, dg), total in zip(plan, totals):
+            tasks = torch.empty(int(total) * 2, dtype=torch.int32, device=dev)
+            # named so that the int32 copies outlive the launch that reads them
+            bra32, qs32, dg32 = bra.to(torch.int32), qs.to(torch.int32), dg.to(torch.int32)
+            _lib.call("pcg_expand_tasks", bra.numel(), _ptr(bra32), _ptr(ket32), _ptr(off), _ptr(qs32), _ptr(dg32),
+                      int(total), _ptr(tasks), _stream())
+            self.classes.setdefault(cls, {})[part] = (tasks, int(total))
+        self.classes = dict(sorted(self.classes.items()))
+        self._task_stats()
+        return self.classes
+
+    def _task_stats(self):
+        nq64 = sum(rec["64"][1] for rec in self.classes.values() if "64" in rec)
+        nq32 = sum(rec["32"][1] for rec in self.classes.values() if "32" in rec)
         # primitive quartets per class and part (for the algorithmic flop count)
         self.prim_quartets = {}
         npp = self.pd["npp"].to(torch.int64)
@@ -247,7 +275,6 @@ class GpuEngine:
         self.stats["quartets_fp64"] = nq64
         self.stats["quartets_fp32"] = nq32
         self.stats["quartets"] = nq64 + nq32
-        return self.classes
 
     def compute_eris(self):
         """Compute every screened quartet block into the in-core class stores."""

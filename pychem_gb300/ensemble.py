@@ -137,76 +137,10 @@ class EnsembleEngine(GpuEngine):
         self.S, self.H = S, H
         return S, H
 
-    def _segments(self, ids):
-        mol = self.pair_mol[ids]
-        starts = np.searchsorted(mol, np.arange(self.B), side="left")
-        ends = np.searchsorted(mol, np.arange(self.B), side="right")
-        return mol, starts, ends
-
-    def build_tasks(self):
-        """As GpuEngine.build_tasks, with every quartet inside one molecule: within a
-        pair kind the pairs are ordered by (molecule, -Q), so the kets of a bra are a
-        prefix of its molecule's segment."""
-        Qh = self.Q.cpu().numpy()
-        thr, thr32 = self.threshold, self.fp32_below
-        kp, ks = [], []
-        for k in range(len(self.kinds)):
-            ids = np.nonzero(self.pair_kind == k)[0]
-            o = np.lexsort((-Qh[ids], self.pair_mol[ids]))
-            kp.append(ids[o].astype(np.int32))
-            ks.append(Qh[ids[o]])
-        self.kind_pairs_dev = [self._t(x) for x in kp]
-        qmax = float(Qh.max()) + 1.0
-        span = 2.0 * qmax + 1.0
-
-        def prefix_count(bra_ids, Qr, ket_ids, Qk, t):
-            kmol, kst, ken = self._segments(ket_ids)
-            bmol = self.pair_mol[bra_ids]
-            key = kmol * span + (qmax - Qk)
-            q = bmol * span + qmax - t / np.maximum(Qr, 1e-300)
-            c = np.searchsorted(key, q, side="left")
-            lo, hi = kst[bmol], ken[bmol]
-            c = np.clip(c, lo, hi)
-            nk = len(Qk)
-            for _ in range(3):   # exact predicate Qr*Qk > t at the boundary
-                up = (c < hi) & (Qr * Qk[np.minimum(c, nk - 1)] > t)
-                c = c + up
-                dn = (c > lo) & ~(Qr * Qk[np.maximum(c - 1, 0)] > t)
-                c = c - dn
-            return (c - lo).astype(np.int64), lo.astype(np.int64)
-
-        per_class = {}
-        nk = len(self.kinds)
-        for kb in range(nk):
-            for kk in range(kb + 1):
-                bra_ids, ket_ids = kp[kb], kp[kk]
-                if len(bra_ids) == 0 or len(ket_ids) == 0:
-                    continue
-                la, lb = int(self.h_pairs["lA"][bra_ids[0]]), int(self.h_pairs["lB"][bra_ids[0]])
-                lc, ld = int(self.h_pairs["lA"][ket_ids[0]]), int(self.h_pairs["lB"][ket_ids[0]])
-                cls = _lib.load().pcg_eri_class_id(la, lb, lc, ld)
-                Qr, Qk = ks[kb], ks[kk]
-                c, seg0 = prefix_count(bra_ids, Qr, ket_ids, Qk, thr)
-                if thr32 > 0:
-                    c32, _ = prefix_count(bra_ids, Qr, ket_ids, Qk, thr32)
-                else:
-                    c32 = c.copy()
-                c32 = np.minimum(c32, c)
-                if kb == kk:
-                    r = np.arange(len(Qr), dtype=np.int64) - seg0
-                    cnt = np.minimum(r + 1, c)
-                    diag = (c <= r).astype(np.int32)
-                    c64 = np.minimum(cnt, c32)
-                else:
-                    cnt = c
-                    diag = np.zeros(len(Qr), dtype=np.int32)
-                    c64 = c32
-                entry = per_class.setdefault(cls, {"64": [], "32": []})
-                entry["64"].append((kb, kk, c64 + diag, seg0.astype(np.int32), diag))
-                if (cnt - c64).sum() > 0:
-                    entry["32"].append((kb, kk, cnt - c64, (seg0 + c64).astype(np.int32),
-                                        np.zeros(len(Qr), dtype=np.int32)))
-        return self._expand(per_class)
+    def _pair_molecule(self):
+        if getattr(self, "_pair_mol_dev", None) is None:
+            self._pair_mol_dev = torch.as_tensor(self.pair_mol, dtype=torch.int64, device=self.dev)
+        return self._pair_mol_dev, self.B
 
     # ---------------------------------------------------------------------------------
     def fock(self, D, out=None, G=None):
