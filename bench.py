@@ -210,26 +210,29 @@ def probe_peak(torch, _lib, fp32):
 
 def ensemble_leg(torch, args, n=1024):
     """1024 perturbed H2O/NH3/CH4/HF/CH3OH/C2H6 (6-31G, 11-30 AO) in one batched SCF,
-    against looping the one-molecule GPU SCF over a sample of the same ensemble."""
+    against looping the one-molecule GPU SCF over a sample of the same ensemble.  Both
+    sides are timed from Molecule objects to converged energies, host set-up included."""
     from pychem_gb300 import workloads as W
     from pychem_gb300.engine import GpuEngine
     from pychem_gb300.ensemble import EnsembleEngine, rhf_batched
     from pychem_gb300.molecule import Molecule
     from pychem_gb300.scf import rhf
     mols = [Molecule(c, "6-31G") for c in W.ensemble(n=n, seed=SEED)]
-    eng = EnsembleEngine(mols)
-    times, res = [], None
+    times, dev_t, res, eng = [], [], None, None
     for k in range(args.warmup + max(1, args.steps)):
+        del eng
         torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng = EnsembleEngine(mols)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        eng.compute_pair_data()
-        eng.one_electron(); eng.schwarz(); eng.build_tasks(); eng.compute_eris()
+        eng.prepare()
         res = rhf_batched(eng)
         e1.record()
         torch.cuda.synchronize()
         if k >= args.warmup:
-            times.append(e0.elapsed_time(e1) / 1e3)
+            times.append(time.perf_counter() - t0)
+            dev_t.append(e0.elapsed_time(e1) / 1e3)
     t_batch = statistics.mean(times)
     sample = mols[:24]
     loop_t = []
@@ -244,11 +247,70 @@ def ensemble_leg(torch, args, n=1024):
     per = min(loop_t) / len(sample)
     dE = max(abs(a - b) for a, b in zip(E_loop, res.E[:len(sample)]))
     return {"workload": "1024 instances cycling H2O, NH3, CH4, HF, CH3OH, C2H6, 6-31G, N(0, 0.08 A) jitter",
-            "instances": n, "batched_s": t_batch, "instances_per_s": n / t_batch,
-            "looped_instances_per_s": 1.0 / per, "speedup_vs_loop": per * n / t_batch,
-            "converged": int(res.converged.sum()), "max_scf_iterations": int(res.iterations.max()),
-            "quartets": eng.stats["quartets"], "max_dE_vs_loop": dE,
-            "loop_sample": "first %d instances, one GpuEngine + rhf each" % len(sample)}
+            "instances": n, "batched_s": t_batch, "batched_device_s": statistics.mean(dev_t),
+            "instances_per_s": n / t_batch, "looped_instances_per_s": 1.0 / per, "speedup_vs_loop": per * n / t_batch,
+            "converged": int(res.converged.sum()), "mean_scf_iterations": float(res.iterations.mean()),
+            "max_scf_iterations": int(res.iterations.max()), "quartets": eng.stats["quartets"],
+            "max_dE_vs_loop": dE, "loop_sample": "first %d instances, one GpuEngine + rhf each" % len(sample)}
+
+
+def learned_leg(torch, args, n=1024):
+    """Held-out generated molecules (<= 6 heavy atoms from C/N/O plus H, N(0, 0.1 A)
+    jitter, seed 2, never seen in training), 6-31G, one batch: plain FP64 batched SCF
+    from the SAD guess against the learned-guess, mixed-precision batched SCF (quartets
+    with Schwarz bound below 1e-4 in FP32), and against looping the plain FP64
+    one-molecule GPU SCF.  Timed from Molecule objects to converged energies."""
+    import numpy as np
+    from pychem_gb300.engine import GpuEngine
+    from pychem_gb300.ensemble import EnsembleEngine, rhf_batched
+    from pychem_gb300.learned.mlp import PairMLP
+    from pychem_gb300.learned.molgen import molecules
+    from pychem_gb300.learned.train import WEIGHTS, guess_density
+    from pychem_gb300.molecule import Molecule
+    from pychem_gb300.scf import rhf
+    if not os.path.exists(WEIGHTS):
+        return {"unavailable": "no trained weights"}
+    net = PairMLP.load(WEIGHTS)
+    mols = [Molecule(c, "6-31G") for c in molecules(n, seed=2)]
+
+    def plain():
+        eng = EnsembleEngine(mols).prepare()
+        return eng, rhf_batched(eng, guess="sad")
+
+    def learned():
+        eng = EnsembleEngine(mols, precision="mixed", fp32_below=1e-4).prepare()
+        return eng, rhf_batched(eng, D0=guess_density(net, mols, eng))
+
+    out = {"workload": "%d held-out generated molecules (<= 6 heavy atoms C/N/O + H), 6-31G, up to %d AO"
+                       % (n, max(m.NOrbitals for m in mols))}
+    res = {}
+    for name, fn in (("plain_fp64_sad", plain), ("learned_mixed", learned)):
+        ts = []
+        for k in range(1 + max(1, min(args.steps, 2))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eng, r = fn()
+            torch.cuda.synchronize()
+            if k >= 1:
+                ts.append(time.perf_counter() - t0)
+            del eng
+        res[name] = r
+        out[name] = {"ttc_s": statistics.mean(ts), "instances_per_s": n / statistics.mean(ts),
+                     "mean_scf_iterations": float(r.iterations.mean()), "max_scf_iterations": int(r.iterations.max()),
+                     "converged": int(r.converged.sum())}
+    dE = res["learned_mixed"].E - res["plain_fp64_sad"].E
+    out["max_abs_dE_learned_mixed_vs_plain"] = float(np.abs(dE).max())
+    out["ttc_ratio_plain_over_learned_mixed"] = out["plain_fp64_sad"]["ttc_s"] / out["learned_mixed"]["ttc_s"]
+    sample = mols[:16]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    E_loop = [rhf(GpuEngine(m).prepare()).E for m in sample]
+    torch.cuda.synchronize()
+    per = (time.perf_counter() - t0) / len(sample)
+    out["looped_plain_fp64_instances_per_s"] = 1.0 / per
+    out["ttc_ratio_looped_plain_over_learned_mixed"] = per * n / out["learned_mixed"]["ttc_s"]
+    out["max_abs_dE_loop_vs_learned_mixed"] = float(max(abs(a - b) for a, b in zip(E_loop, res["learned_mixed"].E)))
+    return out
 
 
 def alkane_leg(torch, args):
@@ -406,6 +468,7 @@ def gpu_arm(args):
 
     ens = ensemble_leg(torch, args) if world == 1 or rank == 0 else None
     alk = alkane_leg(torch, args) if world == 1 or rank == 0 else None
+    lrn = learned_leg(torch, args) if world == 1 or rank == 0 else None
 
     # max over ranks
     if world > 1:
@@ -455,6 +518,7 @@ def gpu_arm(args):
         "cpu_baseline": cpu,
         "ensemble": ens,
         "alkane_mixed": alk,
+        "learned_guess": lrn,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": out["h2d_bytes"],
                 "d2h_bytes_per_step": out["d2h_bytes"]},
         "gpu_launches": launches,

@@ -31,6 +31,31 @@ def basis_library():
     return _basis_cache
 
 
+_shell_cache = {}
+
+
+def element_shells(basis, sym):
+    """(l, exponents, contraction coefficients) of every shell of an element, from the
+    basis library, shared read-only between molecules."""
+    key = (basis, sym)
+    if key not in _shell_cache:
+        data = basis_library()[basis]
+        if sym not in data:
+            raise ValueError("element %s not in basis %s" % (sym, basis))
+        out = []
+        for fn in data[sym]:
+            l = int(fn[0])
+            if l > MAX_L:
+                raise NotImplementedError("shells above d are not supported (l=%d)" % l)
+            exps = np.array([p[0] for p in fn[1:]], dtype=np.float64)
+            ccs = np.array([p[1] for p in fn[1:]], dtype=np.float64)
+            exps.flags.writeable = False
+            ccs.flags.writeable = False
+            out.append((l, exps, ccs))
+        _shell_cache[key] = out
+    return _shell_cache[key]
+
+
 def clean_basis_name(name):
     """Upstream remove_punctuation (Util/structures.py:975-977)."""
     return name.replace("*", "s").replace("-", "").replace("(", "").replace(")", "").replace(",", "").upper()
@@ -48,7 +73,6 @@ class Molecule:
         lib = basis_library()
         if self.Basis not in lib:
             raise ValueError("basis set %s not available (have %s)" % (basis, sorted(lib)))
-        data = lib[self.Basis]
         self.Charge = charge
         self.Multiplicity = multiplicity
         self.atoms = []
@@ -58,15 +82,7 @@ class Molecule:
         self.NAtom = len(self.atoms)
         shells = []
         for ia, (sym, Z, xyz) in enumerate(self.atoms):
-            if sym not in data:
-                raise ValueError("element %s not in basis %s" % (sym, self.Basis))
-            for fn in data[sym]:
-                l = int(fn[0])
-                if l > MAX_L:
-                    raise NotImplementedError("shells above d are not supported (l=%d)" % l)
-                exps = np.array([p[0] for p in fn[1:]], dtype=np.float64)
-                ccs = np.array([p[1] for p in fn[1:]], dtype=np.float64)
-                shells.append((l, exps, ccs, ia))
+            shells += [(l, exps, ccs, ia) for l, exps, ccs in element_shells(self.Basis, sym)]
         self.shells = shells
         self.NCgtf = len(shells)
         ao = 0
@@ -84,19 +100,26 @@ class Molecule:
 
     # -- flat arrays for the device ---------------------------------------------------
     def arrays(self):
-        sh_l = np.array([s[0] for s in self.shells], dtype=np.int32)
-        sh_nprim = np.array([len(s[1]) for s in self.shells], dtype=np.int32)
+        """Flat shell/primitive/atom arrays for the device (computed once)."""
+        if getattr(self, "_arrays", None) is not None:
+            return self._arrays
+        sh = self.shells
+        sh_l = np.array([s[0] for s in sh], dtype=np.int32)
+        sh_nprim = np.array([len(s[1]) for s in sh], dtype=np.int32)
         sh_prim = np.concatenate([[0], np.cumsum(sh_nprim)[:-1]]).astype(np.int32)
         sh_ao = np.array(self.sh_ao, dtype=np.int32)
-        sh_atom = np.array([s[3] for s in self.shells], dtype=np.int32)
-        sh_xyz = np.array([self.atoms[s[3]][2] for s in self.shells], dtype=np.float64).reshape(-1, 3)
-        pr_exp = np.concatenate([s[1] for s in self.shells])
-        pr_cc = np.concatenate([s[2] * (2.0 * s[1]) ** ((s[0] + 1.5) / 2.0) * pure_norm(s[0]) for s in self.shells])
+        sh_atom = np.array([s[3] for s in sh], dtype=np.int32)
         at_xyz = np.array([a[2] for a in self.atoms], dtype=np.float64).reshape(-1, 3)
+        sh_xyz = at_xyz[sh_atom]
+        pr_exp = np.concatenate([s[1] for s in sh])
+        lp = np.repeat(sh_l, sh_nprim)
+        norm = np.array([pure_norm(l) for l in range(MAX_L + 1)])
+        pr_cc = np.concatenate([s[2] for s in sh]) * (2.0 * pr_exp) ** ((lp + 1.5) / 2.0) * norm[lp]
         at_z = np.array([a[1] for a in self.atoms], dtype=np.float64)
-        return dict(sh_l=sh_l, sh_nprim=sh_nprim, sh_prim=sh_prim, sh_ao=sh_ao, sh_atom=sh_atom,
-                    sh_xyz=np.ascontiguousarray(sh_xyz), pr_exp=pr_exp, pr_cc=pr_cc,
-                    at_xyz=np.ascontiguousarray(at_xyz), at_z=at_z)
+        self._arrays = dict(sh_l=sh_l, sh_nprim=sh_nprim, sh_prim=sh_prim, sh_ao=sh_ao, sh_atom=sh_atom,
+                            sh_xyz=np.ascontiguousarray(sh_xyz), pr_exp=pr_exp, pr_cc=pr_cc,
+                            at_xyz=np.ascontiguousarray(at_xyz), at_z=at_z)
+        return self._arrays
 
     def atom_nao(self):
         """Number of AOs of each atom (an atom's AOs are contiguous)."""
@@ -106,13 +129,13 @@ class Molecule:
         return n
 
     def nuclear_repulsion(self):
-        """Methods/integrals.py:196-207."""
-        e = 0.0
-        for i in range(self.NAtom):
-            for j in range(i):
-                r = float(np.linalg.norm(self.atoms[i][2] - self.atoms[j][2]))
-                e += self.atoms[i][1] * self.atoms[j][1] / r
-        return e
+        """Methods/integrals.py:196-207 (sum over atom pairs of Z_i Z_j / r_ij)."""
+        if getattr(self, "_enuc", None) is None:
+            xyz = np.array([a[2] for a in self.atoms], dtype=np.float64).reshape(-1, 3)
+            z = np.array([a[1] for a in self.atoms], dtype=np.float64)
+            i, j = np.tril_indices(self.NAtom, -1)
+            self._enuc = float(np.sum(z[i] * z[j] / np.linalg.norm(xyz[i] - xyz[j], axis=1)))
+        return self._enuc
 
     def coords_list(self, units="BOHR"):
         s = 1.0 if units.upper() == "BOHR" else 1.0 / TO_BOHR
