@@ -258,8 +258,9 @@ def learned_leg(torch, args, n=1024):
     """Held-out generated molecules (<= 6 heavy atoms from C/N/O plus H, N(0, 0.1 A)
     jitter, seed 2, never seen in training), 6-31G, one batch: plain FP64 batched SCF
     from the SAD guess against the learned-guess, mixed-precision batched SCF (quartets
-    with Schwarz bound below 1e-4 in FP32), and against looping the plain FP64
-    one-molecule GPU SCF.  Timed from Molecule objects to converged energies."""
+    with Schwarz bound below 1e-4 in FP32; dense steps in FP32 until the DIIS residual
+    RMS is below 1e-4), and against looping the plain FP64 one-molecule GPU SCF.  Timed
+    from Molecule objects to converged energies."""
     import numpy as np
     from pychem_gb300.engine import GpuEngine
     from pychem_gb300.ensemble import EnsembleEngine, rhf_batched
@@ -279,7 +280,7 @@ def learned_leg(torch, args, n=1024):
 
     def learned():
         eng = EnsembleEngine(mols, precision="mixed", fp32_below=1e-4).prepare()
-        return eng, rhf_batched(eng, D0=guess_density(net, mols, eng))
+        return eng, rhf_batched(eng, D0=guess_density(net, mols, eng), dense_fp32_until=1e-4)
 
     out = {"workload": "%d held-out generated molecules (<= 6 heavy atoms C/N/O + H), 6-31G, up to %d AO"
                        % (n, max(m.NOrbitals for m in mols))}

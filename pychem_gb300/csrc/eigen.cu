@@ -184,11 +184,21 @@ extern "C" int pcg_jacobi_eigh(int batch, int n, const double* A, double* w, voi
     k_jacobi<double, true><<<batch, threads, smem, s>>>(n, m, A, sA, (double*)V, sV, (const double*)V0, w, sw,
                                                          max_sweeps, tol, info);
   } else {
-    const size_t smem = (size_t)m * (m + 1) / 2 * sizeof(float);
-    if (smem > 220 * 1024) { pcg_set_error("pcg_jacobi_eigh: FP32 variant needs n <= 334"); return PCG_ERR_UNSUPPORTED; }
-    PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_jacobi<float, false><<<batch, 1024, smem, s>>>(n, m, A, sA, (float*)V, sV, (const float*)V0, w, sw, max_sweeps,
-                                                      tol, info);
+    // FP32: packed A and V both in shared memory while they fit (n <= 182), else V
+    // in global memory (n <= 334)
+    const size_t smem_v = ((size_t)(m * (m + 1) / 2 + 1) / 2 * 2 + (size_t)m * m) * sizeof(float);
+    if (smem_v <= 200 * 1024 && m / 2 <= 128) {
+      const int threads = m <= 32 ? 128 : 256;
+      PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_v));
+      k_jacobi<float, true><<<batch, threads, smem_v, s>>>(n, m, A, sA, (float*)V, sV, (const float*)V0, w, sw,
+                                                            max_sweeps, tol, info);
+    } else {
+      const size_t smem = (size_t)m * (m + 1) / 2 * sizeof(float);
+      if (smem > 220 * 1024) { pcg_set_error("pcg_jacobi_eigh: FP32 variant needs n <= 334"); return PCG_ERR_UNSUPPORTED; }
+      PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_jacobi<float, false><<<batch, 1024, smem, s>>>(n, m, A, sA, (float*)V, sV, (const float*)V0, w, sw,
+                                                        max_sweeps, tol, info);
+    }
   }
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;

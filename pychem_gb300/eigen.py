@@ -25,7 +25,26 @@ def _stream():
 
 
 def jacobi(A, fp32=False, max_sweeps=40, tol=None):
-    """Unsorted eigenpairs of a batch of symmetric matrices (..., n, n), FP64 input."""
+    """Unsorted eigenpairs of a batch of symmetric matrices (..., n, n), FP64 input and
+    FP64 output (the FP32 variant's vectors converted)."""
+    w, V = _jacobi(A, fp32, max_sweeps, tol)
+    return w, V.to(torch.float64)
+
+
+def eigh32(A, X_prev=None):
+    """Ascending FP32-accurate eigenpairs of symmetric A (..., n, n), n <= 334, with the
+    FP32 Jacobi kernel; with X_prev (orthogonal, float32) the kernel works on
+    X_prev^T A X_prev, which is nearly diagonal between SCF iterations.  Returns
+    (w float64, V float32)."""
+    A = A.to(torch.float32)
+    if X_prev is not None:
+        Ap = X_prev.transpose(-1, -2) @ A @ X_prev
+        w, V = _jacobi(Ap.to(torch.float64), True, 40, None)
+        return _sort(w, X_prev @ V)
+    return _sort(*_jacobi(A.to(torch.float64), True, 40, None))
+
+
+def _jacobi(A, fp32, max_sweeps, tol):
     shape = A.shape
     n = shape[-1]
     A2 = A.reshape(-1, n, n).contiguous()
@@ -38,7 +57,7 @@ def jacobi(A, fp32=False, max_sweeps=40, tol=None):
         tol = 2e-7 if fp32 else 1e-15
     _lib.call("pcg_jacobi_eigh", batch, n, ctypes.c_void_p(A2.data_ptr()), ctypes.c_void_p(w.data_ptr()),
               ctypes.c_void_p(V.data_ptr()), 1 if fp32 else 0, None, max_sweeps, float(tol), None, _stream())
-    return w.reshape(shape[:-1]), V[:, :n, :n].to(torch.float64).reshape(shape)
+    return w.reshape(shape[:-1]), V[:, :n, :n].reshape(shape)
 
 
 def _sort(w, V):

@@ -178,13 +178,12 @@ class GpuEngine:
             setattr(t, f, p[k].data_ptr())
         self.pairs_t = t
         # pair kinds ordered by (pair class, nA, nB)
-        keys = np.stack([pair_class(self.h_pairs["lA"], self.h_pairs["lB"]), nA, nB], axis=1)
-        uniq, inv = np.unique(keys, axis=0, return_inverse=True)
-        order = np.lexsort((uniq[:, 2], uniq[:, 1], uniq[:, 0]))
-        rank = np.empty(len(order), dtype=np.int64)
-        rank[order] = np.arange(len(order))
-        self.kinds = [tuple(int(x) for x in uniq[i]) for i in order]
-        self.pair_kind = rank[np.asarray(inv).ravel()].astype(np.int32)
+        pc = pair_class(self.h_pairs["lA"], self.h_pairs["lB"]).astype(np.int64)
+        ma, mb = int(nA.max()) + 1, int(nB.max()) + 1
+        code = (pc * ma + nA) * mb + nB          # increasing in (pair class, nA, nB)
+        uniq, inv = np.unique(code, return_inverse=True)
+        self.kinds = [(int(c // (ma * mb)), int(c // mb % ma), int(c % mb)) for c in uniq]
+        self.pair_kind = np.asarray(inv).ravel().astype(np.int32)
         self.compute_pair_data()
 
     def compute_pair_data(self):

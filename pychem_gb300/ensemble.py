@@ -144,6 +144,7 @@ class EnsembleEngine(GpuEngine):
 
     # ---------------------------------------------------------------------------------
     def fock(self, D, out=None, G=None):
+        """Batched closed-shell Fock matrices (B, nmax, nmax)."""
         n = self.nmax
         if G is None:
             G = torch.zeros(self.B, n, n, dtype=torch.float64, device=self.dev)
@@ -200,16 +201,50 @@ def sad_batch(eng):
     return D
 
 
-def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="sad", D0=None, compact=0.5):
+def _dense_residual(F, Xa, Xta, Dp, dt):
+    """Fock matrix in the orthonormal basis F' = X^T F X and the DIIS residual
+    R = D'F' - F'D' (= X^T (S D F - F D S) X with D = X D' X^T), in dtype dt."""
+    Fp = Xta.to(dt) @ F.to(dt) @ Xa.to(dt)
+    P = Dp.to(dt) @ Fp
+    return (P - P.transpose(-1, -2)).to(torch.float64)
+
+
+def _dense_density(Fx, Xa, Xta, occa, Q, no, dt):
+    """Eigenvectors Q' of X^T Fx X (dtype dt, starting from the previous Q), the AO
+    density D = C_occ C_occ^T (C = X Q') and the orthonormal-basis density D'."""
+    A = Xta.to(dt) @ Fx.to(dt) @ Xa.to(dt)
+    if dt == torch.float32:
+        _, V = eigen.eigh32(A, X_prev=Q.to(dt) if Q is not None else None)
+    else:
+        _, V = eigen.eigh(A, X_prev=Q)
+    Vo = V[..., :no]
+    mask = occa[:, :no].to(dt).unsqueeze(-2)
+    Co = Xa.to(dt) @ Vo
+    D = (Co * mask) @ Co.transpose(-1, -2)
+    Dp = (Vo * mask) @ Vo.transpose(-1, -2)
+    return V.to(torch.float64), D.to(torch.float64), Dp.to(torch.float64)
+
+
+def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="sad", D0=None, compact=0.5,
+                dense_fp32_until=0.0, trace=None):
     """RHF of every molecule of a prepared EnsembleEngine.  Returns SCFResult with
     per-molecule arrays E, iterations (first iteration meeting the criteria), and C,
     eps, D (batch, nbf_max, ...).
 
     Molecules leave the iteration when they converge: the dense per-molecule work
-    (commutators, DIIS, eigensolver) runs on the still-active rows only, and once the
+    (residuals, DIIS, eigensolver) runs on the still-active rows only, and once the
     active molecules are at most `compact` of those the quartet lists cover, the lists
     and integral stores are cut down to the active molecules (the engine's full lists
-    are restored on return)."""
+    are restored on return).
+
+    dense_fp32_until > 0 (mixed precision): while a molecule's DIIS residual has RMS
+    above this value its dense steps (X^T F X, residual, eigensolver, density) run in
+    FP32; below it, and for every iteration that can declare convergence, in FP64.
+    Fock builds, DIIS extrapolation and energies are FP64 throughout, so the converged
+    state is the FP64 one.
+
+    trace: optional list that receives per iteration (iteration, active molecules, of
+    them in FP32, seconds)."""
     B, n, dev = eng.B, eng.nmax, eng.dev
     S, H = eng.S, eng.H
     e_nuc = np.array([m.nuclear_repulsion() for m in eng.mols])
@@ -217,6 +252,7 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
     for m in eng.mols:
         if m.NAlphaElectrons != m.NBetaElectrons:
             raise ValueError("rhf_batched needs closed-shell molecules")
+    no = int(nocc.max())
     s, U = eigen.eigh(S)
     if float(s.min()) <= 1e-6:
         raise ValueError("linear dependence in an ensemble member; use GpuEngine for it")
@@ -224,19 +260,21 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
     Xt = X.transpose(-1, -2).contiguous()
     occ = (torch.arange(n, device=dev).unsqueeze(0) < nocc.unsqueeze(1)).to(torch.float64)   # (B, n)
 
+    Q = None
     if D0 is not None:
         D = D0.clone()
     elif guess == "sad":
         D = sad_batch(eng)
     else:
-        _, Q0 = eigen.eigh(Xt @ H @ X)
-        C0 = X @ Q0
-        D = (C0 * occ.unsqueeze(-2)) @ C0.transpose(-1, -2)
+        Q, D, _ = _dense_density(H, X, Xt, occ, None, no, torch.float64)
+        Q = None
+    Dp = Xt @ S @ D @ S @ X
     # active rows: molecule ids `act` and their slices of every per-molecule tensor
     act = np.arange(B)
-    Xa, Xta, Sa, Ha, occa, enuc_a = X, Xt, S, H, occ, e_nuc
-    Q = None
-    Dfull = torch.empty_like(S)
+    Xa, Xta, Ha, occa, enuc_a = X, Xt, H, occ, e_nuc
+    p32 = np.full(B, dense_fp32_until > 0)
+    n32 = np.zeros(B, dtype=np.int64)
+    Dfull = torch.zeros_like(S)
     Ffull = torch.empty_like(S)
     Gfull = torch.empty_like(S)
     F_fin = torch.empty_like(S)
@@ -248,22 +286,42 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
     E_at = np.zeros(B)
     covered = B
     it = 0
+    t_last = time.perf_counter()
+
+    def groups(mask):
+        out = []
+        for flag, dt in ((True, torch.float32), (False, torch.float64)):
+            rows = np.nonzero(mask == flag)[0]
+            if len(rows):
+                out.append((None if len(rows) == len(mask) else torch.as_tensor(rows, device=dev), dt))
+        return out
+
+    def take(t, rows):
+        return t if rows is None else t.index_select(0, rows)
+
     try:
         for it in range(1, max_iter + 1):
             act_t = torch.as_tensor(act, device=dev)
             Dfull.index_copy_(0, act_t, D)
             eng.fock(Dfull, out=Ffull, G=Gfull)
             F = Ffull.index_select(0, act_t)
-            R = Xta @ (Sa @ D @ F - F @ D @ Sa) @ Xa
+            R = torch.empty_like(F)
+            for rows, dt in groups(p32):
+                r_ = _dense_residual(take(F, rows), take(Xa, rows), take(Xta, rows), take(Dp, rows), dt)
+                R = r_ if rows is None else R.index_copy_(0, rows, r_)
             Rf = R.reshape(len(act), -1)
             vals = [torch.sum(D * (Ha + F), dim=(1, 2))]
             vals.append(torch.sqrt(torch.mean((D - D_old) ** 2, dim=(1, 2))) if D_old is not None
                         else torch.zeros(len(act), dtype=torch.float64, device=dev))
             vals += [torch.sum(Rf * r.reshape(len(act), -1), dim=1) for r in resids] + [torch.sum(Rf * Rf, dim=1)]
             host = torch.stack(vals, dim=1).cpu().numpy()
+            if trace is not None:
+                now = time.perf_counter()
+                trace.append((it, len(act), int(p32.sum()), now - t_last))
+                t_last = now
             E = host[:, 0] + enuc_a
             if E_old is not None:
-                conv = (np.abs(E - E_old) < e_tol) & (host[:, 1] < d_tol)
+                conv = (np.abs(E - E_old) < e_tol) & (host[:, 1] < d_tol) & ~p32
                 if conv.any():
                     ids = act[conv]
                     ct = torch.as_tensor(np.nonzero(conv)[0], device=dev)
@@ -278,9 +336,9 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
                     keep = ~conv
                     kt = torch.as_tensor(np.nonzero(keep)[0], device=dev)
                     act = act[keep]
-                    D, F, R = D[kt], F[kt], R[kt]
-                    Xa, Xta, Sa, Ha, occa = Xa[kt], Xta[kt], Sa[kt], Ha[kt], occa[kt]
-                    enuc_a, E, host = enuc_a[keep], E[keep], host[keep]
+                    D, Dp, F, R = D[kt], Dp[kt], F[kt], R[kt]
+                    Xa, Xta, Ha, occa = Xa[kt], Xta[kt], Ha[kt], occa[kt]
+                    enuc_a, E, host, p32, n32 = enuc_a[keep], E[keep], host[keep], p32[keep], n32[keep]
                     Q = Q[kt] if Q is not None else None
                     focks = [f[kt] for f in focks]
                     resids = [r[kt] for r in resids]
@@ -291,6 +349,21 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
                         eng.restrict(mask)
                         covered = len(act)
             E_old, D_old = E, D
+            # FP32 dense steps end once the residual is small (or after 16 iterations)
+            rms = np.sqrt(np.maximum(host[:, -1], 0.0) / (n * n))
+            n32 += p32
+            p32_new = p32 & (rms > dense_fp32_until) & (n32 < 16)
+            switched = np.nonzero(p32 & ~p32_new)[0]
+            p32 = p32_new
+            if len(switched) and Q is not None:
+                # FP32-accurate eigenvectors start the FP64 steps: make them orthonormal
+                # to FP64 accuracy (two Newton-Schulz steps of the polar factor)
+                sw = torch.as_tensor(switched, device=dev)
+                Qs = Q.index_select(0, sw)
+                I = torch.eye(n, dtype=torch.float64, device=dev)
+                for _ in range(2):
+                    Qs = Qs @ (1.5 * I - 0.5 * Qs.transpose(-1, -2) @ Qs)
+                Q.index_copy_(0, sw, Qs)
             row = host[:, 2:]
             m = row.shape[1]
             Bn = np.zeros((len(act), m, m))
@@ -308,9 +381,16 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
             if k > 1:
                 cw = torch.tensor(diis_coefficients_batched(Bm), dtype=torch.float64, device=dev)
                 Fx = torch.einsum("bk,kbij->bij", cw, torch.stack(focks))
-            _, Q = eigen.eigh(Xta @ Fx @ Xa, X_prev=Q)
-            C = Xa @ Q
-            D = (C * occa.unsqueeze(-2)) @ C.transpose(-1, -2)
+            Qn, Dn, Dpn = torch.empty_like(F), torch.empty_like(F), torch.empty_like(F)
+            for rows, dt in groups(p32):
+                out = _dense_density(take(Fx, rows), take(Xa, rows), take(Xta, rows), take(occa, rows),
+                                     take(Q, rows) if Q is not None else None, no, dt)
+                if rows is None:
+                    Qn, Dn, Dpn = out
+                else:
+                    for dst, src in zip((Qn, Dn, Dpn), out):
+                        dst.index_copy_(0, rows, src)
+            Q, D, Dp = Qn, Dn, Dpn
     finally:
         eng.unrestrict()
     if len(act):

@@ -62,3 +62,25 @@ def test_refinement_from_previous_vectors(n):
         assert (P3 - U2[:, :nocc] @ U2[:, :nocc].T).abs().max().item() < 1e-11
         I = torch.eye(n, dtype=torch.float64, device="cuda")
         assert (V2.T @ V2 - I).abs().max().item() < 1e-12
+
+
+@pytest.mark.parametrize("n", [13, 82, 181, 182, 190])
+def test_fp32_eigh_with_previous_vectors(n):
+    """FP32 Jacobi (V in shared memory up to n = 182, in global memory above): from
+    scratch and from nearby previous eigenvectors, eigenvalues to FP32 accuracy and an
+    orthogonal eigenvector matrix."""
+    from pychem_gb300 import eigen
+    A = rand_sym(4, n, 11)
+    ref = torch.linalg.eigvalsh(A)
+    scale = max(1.0, ref.abs().max().item())
+    w, V = eigen.eigh32(A)
+    assert V.dtype == torch.float32
+    assert (w - ref).abs().max().item() < 2e-5 * scale * n ** 0.5
+    I = torch.eye(n, dtype=torch.float32, device="cuda")
+    assert (V.transpose(-1, -2) @ V - I).abs().max().item() < 2e-5 * n ** 0.5
+    A2 = A + 1e-3 * rand_sym(4, n, 12)
+    ref2 = torch.linalg.eigvalsh(A2)
+    w2, V2 = eigen.eigh32(A2, X_prev=V)
+    assert (w2 - ref2).abs().max().item() < 2e-5 * scale * n ** 0.5
+    resid = A2.float() @ V2 - V2 * w2.float().unsqueeze(-2)
+    assert resid.abs().max().item() < 1e-4 * scale * n ** 0.5

@@ -69,3 +69,16 @@ def test_compaction_changes_nothing(ensemble):
     assert np.abs(r_never.E - r_always.E).max() < 1e-12
     assert np.abs(r_never.E - res.E).max() < 1e-12
     assert (r_always.D - r_never.D).abs().max().item() < 1e-10
+
+
+def test_fp32_dense_phase_reaches_the_fp64_state(ensemble):
+    """Mixed-precision dense steps (FP32 until the DIIS residual RMS drops below 1e-4)
+    converge every molecule to the FP64 energies."""
+    from pychem_gb300.ensemble import rhf_batched
+    mols, eng, res = ensemble
+    trace = []
+    r = rhf_batched(eng, dense_fp32_until=1e-4, trace=trace)
+    assert r.converged.all()
+    assert np.abs(r.E - res.E).max() < 1e-9
+    assert trace[0][2] == len(mols)          # every molecule starts in FP32
+    assert trace[-1][2] == 0
