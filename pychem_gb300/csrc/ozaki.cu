@@ -14,16 +14,19 @@
 //     arithmetic is involved (GB300's FP64 pipe is ~1/60 of its FP32 pipe).
 //  2. Slice products A_p B_q are integer matrices computed on the tensor cores with FP32
 //     accumulation (products of 8-bit integers are exact in FP32).  Products of one level
-//     L = p + q (p, q <= s, L <= s + 1) share the scale 2^{-beta L} and are summed in
-//     one FP32 buffer, exact while K (2 * 2^13 + (s - 2) 2^12) < 2^24, i.e.
-//     K (s + 2) < 4096 (checked; K = 298 allows s <= 11).
+//     L = p + q (p, q <= s, L <= s + 1) share the scale 2^{-beta L}; the slices are
+//     stored so that a level is ONE GEMM over the concatenated inner dimension
+//     (A_{p_lo} .. A_{p_hi}) x (B_{L-p_lo}; ..; B_{L-p_hi}): A slices row-interleaved
+//     [vector][p][k], B slices in descending order [batch][s - q][k][n].  The level sum
+//     is exact in FP32 while K (2 * 2^13 + (s - 2) 2^12) < 2^24, i.e. K (s + 2) < 4096
+//     (checked; K = 298 allows s <= 11).
 //  3. Every level has its own FP32 buffer; one pass combines them exactly in int64,
 //     acc = sum_L P_L 2^{beta (s+1-L)} (|acc| < 2^60), and writes
 //     C = acc 2^{eA + eB - beta (s+1)} (one int64->FP64 conversion per element).
 // Dropped terms (p + q > s + 1) bound the relative error of an element by about
 // K 2^{-beta s} of (row max of A) * (column max of B).
 //
-// The slice GEMMs are plain library GEMMs (cuBLAS, BF16 in, FP32 out); splitting and
+// The level GEMMs are plain library GEMMs (cuBLAS, BF16 in, FP32 out); splitting and
 // FP64 accumulation are the kernels below.
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
@@ -35,6 +38,7 @@
 #include "pcg_internal.h"
 
 #define OZ_BETA 7
+#define OZ_THREADS 256
 
 static cublasHandle_t g_cublas[64];
 
@@ -49,100 +53,128 @@ static int get_cublas(cublasHandle_t* h) {
   return PCG_OK;
 }
 
-// Split: one CTA per OZ_VB consecutive vectors.  Vector v = (v1, v0) holds elements
-// src[v1*s1 + v0*s0 + k*ks], k < K; the CTA stages its OZ_VB x K tile in shared memory
-// (coalesced along whichever of s0 / ks is 1), finds each vector's exponent, then
-// writes the digits of every element to the nslice slice arrays (same layout as src).
-#define OZ_VB 32
-#define OZ_THREADS 256
-
 __device__ __forceinline__ unsigned long long oz_absbits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
 
-__global__ void __launch_bounds__(OZ_THREADS) k_oz_split(const double* __restrict__ src, long long n1, long long s1,
-                                                         long long n0, long long s0, int K, long long ks, int nslice,
-                                                         __nv_bfloat16* __restrict__ slices, long long slice_stride,
-                                                         int* __restrict__ exps) {
-  extern __shared__ double tile[];  // [OZ_VB][K]
-  __shared__ unsigned long long vmax[OZ_VB];
-  const long long nv = n1 * n0;
-  const long long vbase = (long long)blockIdx.x * OZ_VB;
-  const int nvl = (int)min((long long)OZ_VB, nv - vbase);
-  const bool vec_fast = (s0 == 1);  // consecutive threads -> consecutive vectors
-  const int total = OZ_VB * K;
-  for (int idx = threadIdx.x; idx < total; idx += OZ_THREADS) {
-    int vl, k;
-    if (vec_fast) { vl = idx % OZ_VB; k = idx / OZ_VB; } else { vl = idx / K; k = idx % K; }
-    double x = 0.0;
-    if (vl < nvl) {
-      const long long v = vbase + vl;
-      x = src[(v / n0) * s1 + (v % n0) * s0 + (long long)k * ks];
-    }
-    tile[vl * K + k] = x;
+// The NS signed digits of x for the exponent field emax of its vector's max.
+template <int NS>
+__device__ __forceinline__ void oz_digits(double x, int emax, int* d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int e = emax ? emax - 1022 : 0;  // max < 2^e
+  const int ex = (int)((u >> 52) & 0x7FF);
+  unsigned long long F = 0;
+  if (ex != 0 && emax != 0) {
+    const unsigned long long mant = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = ex - 1012 - e;  // F = mant 2^sh < 2^63
+    if (sh >= 0) F = mant << sh;
+    else if (sh > -64) F = mant >> (-sh);
   }
-  __syncthreads();
-  // per-vector max |x| as an integer compare of the magnitude bit patterns
-  {
-    const int g = OZ_THREADS / OZ_VB;  // threads per vector
-    const int vl = threadIdx.x / g, lane = threadIdx.x % g;
-    unsigned long long m = 0;
-    for (int k = lane; k < K; k += g) m = max(m, oz_absbits(tile[vl * K + k]));
-    for (int off = g / 2; off > 0; off >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, off, g));
-    if (lane == 0) vmax[vl] = m;
+  const int lowbit = 63 - OZ_BETA * NS;  // first bit below the last digit
+#pragma unroll
+  for (int p = 1; p <= NS; ++p) d[p - 1] = (int)((F >> (63 - OZ_BETA * p)) & 127ull);
+  if (lowbit >= 1) d[NS - 1] += (int)((F >> (lowbit - 1)) & 1ull);  // round the last digit
+  int carry = 0;
+#pragma unroll
+  for (int p = NS - 1; p >= 1; --p) {
+    const int t = d[p] + carry;
+    carry = t >= 64 ? 1 : 0;
+    d[p] = t - 128 * carry;
   }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < total; idx += OZ_THREADS) {
-    int vl, k;
-    if (vec_fast) { vl = idx % OZ_VB; k = idx / OZ_VB; } else { vl = idx / K; k = idx % K; }
-    if (vl >= nvl) continue;
-    const unsigned long long mb = vmax[vl];
-    const int emax = (int)(mb >> 52);                 // exponent field of the vector max
-    const int e = emax ? emax - 1022 : 0;             // max < 2^e
-    const long long v = vbase + vl;
-    if (k == 0) exps[v] = e;
-    const unsigned long long u = (unsigned long long)__double_as_longlong(tile[vl * K + k]);
-    const int ex = (int)((u >> 52) & 0x7FF);
-    unsigned long long F = 0;
-    if (ex != 0 && emax != 0) {
-      const unsigned long long mant = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-      const int sh = ex - 1012 - e;                   // F = mant 2^sh < 2^63
-      if (sh >= 0) F = mant << sh;
-      else if (sh > -64) F = mant >> (-sh);
-    }
-    int d[8];
-    const int lowbit = 63 - 7 * nslice;               // first bit below the last digit
-    for (int p = 1; p <= nslice; ++p) d[p - 1] = (int)((F >> (63 - 7 * p)) & 127ull);
-    if (lowbit >= 1) d[nslice - 1] += (int)((F >> (lowbit - 1)) & 1ull);  // round the last digit
-    int carry = 0;
-    for (int p = nslice - 1; p >= 1; --p) {
-      int t = d[p] + carry;
-      carry = t >= 64 ? 1 : 0;
-      d[p] = t - 128 * carry;
-    }
-    d[0] += carry;
-    const bool neg = (u >> 63) != 0;
-    const long long off = (v / n0) * s1 + (v % n0) * s0 + (long long)k * ks;
-    for (int p = 0; p < nslice; ++p)
-      slices[(long long)p * slice_stride + off] = __int2bfloat16_rn(neg ? -d[p] : d[p]);
+  d[0] += carry;
+  if ((u >> 63) != 0) {
+#pragma unroll
+    for (int p = 0; p < NS; ++p) d[p] = -d[p];
+  }
+}
+
+// Split.  A vector is one row of A or one column of B over k: vector (v1, v0) holds
+// src[v1*s1 + v0*s0 + k*ks], k < K (v1 the batch).  Its exponent e (max |x| < 2^e)
+// comes from an integer max of the magnitude bit patterns; the digits of each element
+// then go to the slice layout of the operand's role:
+//   role A: out[((v1 * n0 + v0) * NS + p - 1) * K + k]
+//   role B: out[((v1 * NS + NS - p) * K + k) * n0 + v0]
+template <int NS>
+__device__ __forceinline__ long long oz_out(bool roleA, long long v1, long long v0, long long n0, int K, int p, int k) {
+  return roleA ? ((v1 * n0 + v0) * NS + p - 1) * K + k : ((v1 * NS + NS - p) * (long long)K + k) * n0 + v0;
+}
+
+// Vectors contiguous (s0 == 1): one thread per vector; each k is one coalesced row of
+// consecutive vectors; the digit pass re-reads the column from L2.
+template <int NS>
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_split_v(const double* __restrict__ src, long long n1,
+                                                           long long s1, long long n0, int K, long long ks,
+                                                           int roleA, __nv_bfloat16* __restrict__ out,
+                                                           int* __restrict__ exps) {
+  const long long chunks = (n0 + OZ_THREADS - 1) / OZ_THREADS;
+  const long long v1 = blockIdx.x / chunks;
+  const long long v0 = (blockIdx.x % chunks) * OZ_THREADS + threadIdx.x;
+  if (v1 >= n1 || v0 >= n0) return;
+  const double* x = src + v1 * s1 + v0;
+  unsigned long long m = 0;
+#pragma unroll 8
+  for (int k = 0; k < K; ++k) m = max(m, oz_absbits(__ldg(x + (long long)k * ks)));
+  const int emax = (int)(m >> 52);
+  exps[v1 * n0 + v0] = emax ? emax - 1022 : 0;
+#pragma unroll 4
+  for (int k = 0; k < K; ++k) {
+    int d[NS];
+    oz_digits<NS>(__ldg(x + (long long)k * ks), emax, d);
+#pragma unroll
+    for (int p = 1; p <= NS; ++p) out[oz_out<NS>(roleA, v1, v0, n0, K, p, k)] = __int2bfloat16_rn(d[p - 1]);
+  }
+}
+
+// k contiguous (ks == 1): one warp per vector, lanes over k.
+template <int NS>
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_split_k(const double* __restrict__ src, long long n1,
+                                                           long long s1, long long n0, long long s0, int K,
+                                                           int roleA, __nv_bfloat16* __restrict__ out,
+                                                           int* __restrict__ exps) {
+  const long long v = (long long)blockIdx.x * (OZ_THREADS / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (v >= n1 * n0) return;
+  const long long v1 = v / n0, v0 = v % n0;
+  const double* x = src + v1 * s1 + v0 * s0;
+  unsigned long long m = 0;
+  for (int k = lane; k < K; k += 32) m = max(m, oz_absbits(__ldg(x + k)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const int emax = (int)(m >> 52);
+  if (lane == 0) exps[v] = emax ? emax - 1022 : 0;
+  for (int k = lane; k < K; k += 32) {
+    int d[NS];
+    oz_digits<NS>(__ldg(x + k), emax, d);
+#pragma unroll
+    for (int p = 1; p <= NS; ++p) out[oz_out<NS>(roleA, v1, v0, n0, K, p, k)] = __int2bfloat16_rn(d[p - 1]);
   }
 }
 
 // C[b][m][n] (+)= (sum_L P_L[b][m][n] 2^{beta (s+1-L)}) 2^{eA[bA][m] + eB[bB][n] - beta (s+1)}
-__global__ void k_oz_combine(const float* __restrict__ P, long long pstride, int nslice, double* __restrict__ C,
-                             long long batch, int M, int N, long long sCb, const int* __restrict__ eA, int a_batched,
-                             const int* __restrict__ eB, int b_batched, int assign) {
-  const long long total = batch * (long long)M * N;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
+// One CTA per row r = b * M + m and chunk of 4 * OZ_THREADS columns.
+#define OZ_COMBINE_COLS (4 * OZ_THREADS)
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_combine(const float* __restrict__ P, long long pstride, int nslice,
+                                                           double* __restrict__ C, long long rows, int M, int N,
+                                                           long long sCb, const int* __restrict__ eA, int a_batched,
+                                                           const int* __restrict__ eB, int b_batched, int assign) {
+  const long long nch = (N + OZ_COMBINE_COLS - 1) / OZ_COMBINE_COLS;
+  const long long r = blockIdx.x / nch;
+  if (r >= rows) return;
+  const int c0 = (int)(blockIdx.x % nch) * OZ_COMBINE_COLS;
+  const long long b = r / M;
+  const int m = (int)(r % M);
+  const int ea = eA[(a_batched ? b * M : 0) + m] - OZ_BETA * (nslice + 1);
+  const int* eb = eB + (b_batched ? b * N : 0);
+  const float* Pr = P + r * N;
+  double* Cr = C + b * sCb + (long long)m * N;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int n = c0 + j * OZ_THREADS + threadIdx.x;
+    if (n >= N) break;
     long long acc = 0;
     for (int L = 2; L <= nslice + 1; ++L)
-      acc += __float2ll_rn(P[(long long)(L - 2) * pstride + idx]) << (OZ_BETA * (nslice + 1 - L));
-    const int n = (int)(idx % N);
-    const long long t = idx / N;
-    const int m = (int)(t % M);
-    const long long b = t / M;
-    const int e = eA[(a_batched ? b * M : 0) + m] + eB[(b_batched ? b * N : 0) + n] - OZ_BETA * (nslice + 1);
+      acc += __float2ll_rn(__ldg(Pr + (long long)(L - 2) * pstride + n)) << (OZ_BETA * (nslice + 1 - L));
+    const int e = ea + __ldg(eb + n);
     double v = 0.0;
     if (acc != 0) {
       // exact power-of-two scaling by adding to the exponent field (no FP64 multiply)
@@ -151,13 +183,8 @@ __global__ void k_oz_combine(const float* __restrict__ P, long long pstride, int
       if (ef <= 0) v = 0.0;  // below the normal range: far under any tolerance here
       else { bits = (bits & ~(0x7FFll << 52)) | ((long long)ef << 52); v = __longlong_as_double(bits); }
     }
-    double* c = C + b * sCb + (long long)m * N + n;
-    *c = assign ? v : *c + v;
+    Cr[n] = assign ? v : Cr[n] + v;
   }
-}
-
-static long long extent(long long nb, long long sb, long long n1, long long s1, long long n2, long long s2) {
-  return (nb - 1) * sb + (n1 - 1) * s1 + (n2 - 1) * s2 + 1;
 }
 
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -170,11 +197,11 @@ struct OzLayout {
 static OzLayout oz_layout(const pcg_gemm_desc_t* d, int s) {
   OzLayout L;
   const long long nbA = d->sAb ? d->batch : 1, nbB = d->sBb ? d->batch : 1;
-  // slice stride rounded to 128 elements so every slice starts 256-byte aligned
-  L.extA = (extent(nbA, d->sAb, d->M, d->sAm, d->K, d->sAk) + 127) / 128 * 128;
-  L.extB = (extent(nbB, d->sBb, d->N, d->sBn, d->K, d->sBk) + 127) / 128 * 128;
   L.nvecA = nbA * d->M;
   L.nvecB = nbB * d->N;
+  // compact slice arrays: s digits of every element of every vector
+  L.extA = (L.nvecA * (long long)d->K + 127) / 128 * 128;
+  L.extB = (L.nvecB * (long long)d->K + 127) / 128 * 128;
   size_t o = 0;
   L.offA = o; o = align256(o + (size_t)s * L.extA * 2);
   L.offB = o; o = align256(o + (size_t)s * L.extB * 2);
@@ -184,6 +211,36 @@ static OzLayout oz_layout(const pcg_gemm_desc_t* d, int s) {
   L.offP = o; o = align256(o + (size_t)s * L.pstride * 4);
   L.total = o;
   return L;
+}
+
+template <int NS>
+static void oz_launch_split(const double* src, long long nb, long long sb, long long nv0, long long sv0, long long sk,
+                            int K, int roleA, __nv_bfloat16* out, int* ex, cudaStream_t s) {
+  // by k when k is contiguous and the vectors are not (or for A, whose slices run along k)
+  if (sk == 1 && (roleA || sv0 != 1)) {
+    const long long per = OZ_THREADS / 32;
+    k_oz_split_k<NS><<<(unsigned)((nb * nv0 + per - 1) / per), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, sv0, K, roleA,
+                                                                                  out, ex);
+  } else {
+    const long long chunks = (nv0 + OZ_THREADS - 1) / OZ_THREADS;
+    k_oz_split_v<NS><<<(unsigned)(nb * chunks), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, K, sk, roleA, out, ex);
+  }
+}
+
+static int oz_split(int nslice, const double* src, long long nb, long long sb, long long nv0, long long sv0,
+                    long long sk, int K, int roleA, __nv_bfloat16* out, int* ex, cudaStream_t s) {
+  switch (nslice) {
+    case 1: oz_launch_split<1>(src, nb, sb, nv0, sv0, sk, K, roleA, out, ex, s); break;
+    case 2: oz_launch_split<2>(src, nb, sb, nv0, sv0, sk, K, roleA, out, ex, s); break;
+    case 3: oz_launch_split<3>(src, nb, sb, nv0, sv0, sk, K, roleA, out, ex, s); break;
+    case 4: oz_launch_split<4>(src, nb, sb, nv0, sv0, sk, K, roleA, out, ex, s); break;
+    case 5: oz_launch_split<5>(src, nb, sb, nv0, sv0, sk, K, roleA, out, ex, s); break;
+    case 6: oz_launch_split<6>(src, nb, sb, nv0, sv0, sk, K, roleA, out, ex, s); break;
+    case 7: oz_launch_split<7>(src, nb, sb, nv0, sv0, sk, K, roleA, out, ex, s); break;
+    default: pcg_set_error("pcg_ozaki_gemm: nslice out of range"); return PCG_ERR_ARG;
+  }
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
 }
 
 extern "C" size_t pcg_ozaki_workspace(const pcg_gemm_desc_t* d, int nslice) {
@@ -202,9 +259,7 @@ extern "C" int pcg_ozaki_gemm(const pcg_gemm_desc_t* d, const double* A, const d
     pcg_set_error("pcg_ozaki_gemm: K too large for exact FP32 level sums (need K * (nslice + 2) < 4096)");
     return PCG_ERR_UNSUPPORTED;
   }
-  const bool a_rowk = d->sAk == 1, a_colm = d->sAm == 1;
-  const bool b_rown = d->sBn == 1, b_colk = d->sBk == 1;
-  if (!(a_rowk || a_colm) || !(b_rown || b_colk)) {
+  if (!(d->sAk == 1 || d->sAm == 1) || !(d->sBn == 1 || d->sBk == 1)) {
     pcg_set_error("pcg_ozaki_gemm: each operand needs a unit stride along one of its two matrix axes");
     return PCG_ERR_ARG;
   }
@@ -220,56 +275,39 @@ extern "C" int pcg_ozaki_gemm(const pcg_gemm_desc_t* d, const double* A, const d
   int* eA = (int*)(ws + L.offEA);
   int* eB = (int*)(ws + L.offEB);
   float* P = (float*)(ws + L.offP);
-  // split A: vectors (b, m) along k; B: vectors (b, n) along k
-  const size_t smem = (size_t)OZ_VB * d->K * sizeof(double);
-  PCG_CUDA(cudaFuncSetAttribute(k_oz_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  {
-    const long long nb = d->sAb ? d->batch : 1;
-    const long long nv = nb * d->M;
-    k_oz_split<<<(unsigned)((nv + OZ_VB - 1) / OZ_VB), OZ_THREADS, smem, s>>>(A, nb, d->sAb, d->M, d->sAm, d->K,
-                                                                             d->sAk, nslice, sa, L.extA, eA);
-    PCG_CUDA(cudaGetLastError());
-  }
-  {
-    const long long nb = d->sBb ? d->batch : 1;
-    const long long nv = nb * d->N;
-    k_oz_split<<<(unsigned)((nv + OZ_VB - 1) / OZ_VB), OZ_THREADS, smem, s>>>(B, nb, d->sBb, d->N, d->sBn, d->K,
-                                                                             d->sBk, nslice, sb, L.extB, eB);
-    PCG_CUDA(cudaGetLastError());
-  }
+  const long long nbA = d->sAb ? d->batch : 1, nbB = d->sBb ? d->batch : 1;
+  if (int rc = oz_split(nslice, A, nbA, d->sAb, d->M, d->sAm, d->sAk, d->K, 1, sa, eA, s)) return rc;
+  if (int rc = oz_split(nslice, B, nbB, d->sBb, d->N, d->sBn, d->sBk, d->K, 0, sb, eB, s)) return rc;
   cublasHandle_t h;
   if (int rc = get_cublas(&h)) return rc;
   if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) { pcg_set_error("cublasSetStream failed"); return PCG_ERR_CUDA; }
-  // column-major call: C_cm (N x M, ld N) = opB(B) (N x K) * opA(A) (K x M)
-  const cublasOperation_t opB = b_rown ? CUBLAS_OP_N : CUBLAS_OP_T;
-  const long long ldb = b_rown ? d->sBk : d->sBn;
-  const cublasOperation_t opA = a_rowk ? CUBLAS_OP_N : CUBLAS_OP_T;
-  const long long lda = a_rowk ? d->sAm : d->sAk;
+  // level L = one GEMM over the inner dimension K_L = (p_hi - p_lo + 1) K; column-major
+  // call: P_L (N x M, ld N) = Bcat (N x K_L, ld N) * Acat (K_L x M, ld s K)
   const float one = 1.0f, zero = 0.0f;
-  const long long total = (long long)d->batch * d->M * d->N;
-  const int threads = 256;
-  const int blocks = (int)((total + threads - 1) / threads > 152 * 64 ? 152 * 64 : (total + threads - 1) / threads);
+  const long long K = d->K;
   for (int lev = 2; lev <= nslice + 1; ++lev) {
-    bool first = true;
+    const int p_lo = lev - nslice > 1 ? lev - nslice : 1;
+    const int p_hi = lev - 1 < nslice ? lev - 1 : nslice;
+    const int kl = (p_hi - p_lo + 1) * (int)K;
+    const __nv_bfloat16* Bcat = sb + (size_t)(nslice - lev + p_lo) * K * d->N;
+    const __nv_bfloat16* Acat = sa + (size_t)(p_lo - 1) * K;
     float* PL = P + (size_t)(lev - 2) * L.pstride;
-    for (int p = 1; p <= nslice; ++p) {
-      const int q = lev - p;
-      if (q < 1 || q > nslice) continue;
-      const cublasStatus_t st = cublasGemmStridedBatchedEx(
-          h, opB, opA, d->N, d->M, d->K, &one, sb + (size_t)(q - 1) * L.extB, CUDA_R_16BF, (int)ldb, d->sBb,
-          sa + (size_t)(p - 1) * L.extA, CUDA_R_16BF, (int)lda, d->sAb, first ? &zero : &one, PL, CUDA_R_32F, d->N,
-          (long long)d->M * d->N, d->batch, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-      if (st != CUBLAS_STATUS_SUCCESS) {
-        char msg[96];
-        snprintf(msg, sizeof(msg), "cublasGemmStridedBatchedEx failed (%d)", (int)st);
-        pcg_set_error(msg);
-        return PCG_ERR_CUDA;
-      }
-      first = false;
+    const cublasStatus_t st = cublasGemmStridedBatchedEx(
+        h, CUBLAS_OP_N, CUBLAS_OP_N, d->N, d->M, kl, &one, Bcat, CUDA_R_16BF, d->N,
+        d->sBb ? (long long)nslice * K * d->N : 0, Acat, CUDA_R_16BF, (int)(nslice * K),
+        d->sAb ? (long long)d->M * nslice * K : 0, &zero, PL, CUDA_R_32F, d->N, (long long)d->M * d->N, d->batch,
+        CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+    if (st != CUBLAS_STATUS_SUCCESS) {
+      char msg[96];
+      snprintf(msg, sizeof(msg), "cublasGemmStridedBatchedEx failed (%d)", (int)st);
+      pcg_set_error(msg);
+      return PCG_ERR_CUDA;
     }
   }
-  k_oz_combine<<<blocks, threads, 0, s>>>(P, L.pstride, nslice, C, d->batch, d->M, d->N, d->sCb, eA, d->sAb ? 1 : 0,
-                                          eB, d->sBb ? 1 : 0, accumulate ? 0 : 1);
+  const long long rows = (long long)d->batch * d->M;
+  const long long nch = (d->N + OZ_COMBINE_COLS - 1) / OZ_COMBINE_COLS;
+  k_oz_combine<<<(unsigned)(rows * nch), OZ_THREADS, 0, s>>>(P, L.pstride, nslice, C, rows, d->M, d->N, d->sCb, eA,
+                                                              d->sAb ? 1 : 0, eB, d->sBb ? 1 : 0, accumulate ? 0 : 1);
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;
 }
