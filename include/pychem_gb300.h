@@ -145,6 +145,10 @@ typedef struct {
   const int *A, *B, *ppoff, *npp_of;
   const double *AB, *zeta, *P, *PA, *K, *oo2z;
   const float *Kf;
+  /* Optional (NULL allowed): per pair 4 ints (first AO of A | (A == B) << 30, first AO
+   * of B, low and high 32 bits of the molecule block offset), filled by pcg_pair_ao;
+   * the Fock digestion reads it instead of the shell tables. */
+  const int *ao4;
 } pcg_pairs_t;
 
 /* Primitive-pair data for npair pairs (replaces the per-pair ShellPair set-up,
@@ -152,6 +156,9 @@ typedef struct {
 int pcg_pair_data(const pcg_basis_t *basis, int npair, const int *A, const int *B,
                   const int *ppoff, double *AB, double *zeta, double *P, double *PA, double *K,
                   float *Kf, double *oo2z, void *stream);
+
+/* The per-pair AO table pcg_pairs_t.ao4 (npair x 4 ints) from the shell tables. */
+int pcg_pair_ao(const pcg_basis_t *basis, int npair, const int *A, const int *B, int *ao4, void *stream);
 
 /* Overlap S and core Hamiltonian H = T + V, nbf x nbf, all shell pairs listed
  * (Methods/hartree_fock.py:207-224 over Methods/integrals.py:220-370). */

@@ -117,6 +117,23 @@ int pcg_launch_pair_data(const DevBasis& b, int npair, const int* pA, const int*
   return PCG_OK;
 }
 
+__global__ void k_pair_ao(DevBasis b, int npair, const int* __restrict__ pA, const int* __restrict__ pB,
+                          int4* __restrict__ ao4) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  const int A = pA[p], B = pB[p];
+  const long long o = dev_blk(b, A);
+  ao4[p] = make_int4(b.sh_ao[A] | (A == B ? 1 << 30 : 0), b.sh_ao[B], (int)(unsigned)(o & 0xFFFFFFFFll),
+                     (int)(o >> 32));
+}
+
+int pcg_launch_pair_ao(const DevBasis& b, int npair, const int* pA, const int* pB, int* ao4, cudaStream_t s) {
+  if (npair <= 0) return PCG_OK;
+  k_pair_ao<<<(npair + 127) / 128, 128, 0, s>>>(b, npair, pA, pB, (int4*)ao4);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
 // ----------------------------------------------------------------------------------
 // One-electron integrals
 // ----------------------------------------------------------------------------------

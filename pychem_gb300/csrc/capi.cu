@@ -35,6 +35,7 @@ static DevPairsExt to_dev(const pcg_pairs_t* p) {
   d.p.npair = p->npair; d.p.npp = p->npp;
   d.p.A = p->A; d.p.B = p->B; d.p.ppoff = p->ppoff; d.p.npp_of = p->npp_of;
   d.p.AB = p->AB; d.p.zeta = p->zeta; d.p.P = p->P; d.p.PA = p->PA; d.p.K = p->K; d.p.Kf = p->Kf;
+  d.p.ao4 = (const int4*)p->ao4;
   d.oo2z = p->oo2z;
   return d;
 }
@@ -56,6 +57,14 @@ int pcg_pair_data(const pcg_basis_t* basis, int npair, const int* A, const int* 
   if (!basis || npair < 0) { pcg_set_error("pcg_pair_data: bad arguments"); return PCG_ERR_ARG; }
   return pcg_launch_pair_data(to_dev(basis), npair, A, B, ppoff, AB, zeta, P, PA, K, Kf, oo2z,
                               (cudaStream_t)stream);
+}
+
+int pcg_pair_ao(const pcg_basis_t* basis, int npair, const int* A, const int* B, int* ao4, void* stream) {
+  if (!basis || npair < 0 || (npair > 0 && (!A || !B || !ao4))) {
+    pcg_set_error("pcg_pair_ao: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  return pcg_launch_pair_ao(to_dev(basis), npair, A, B, ao4, (cudaStream_t)stream);
 }
 
 int pcg_one_electron(const pcg_basis_t* basis, int npair, const int* A, const int* B, double* S, double* H,

@@ -196,4 +196,5 @@ struct DevPairs {
   const double* PA;   // [npp][3]
   const double* K;
   const float* Kf;
+  const int4* ao4;    // optional: (AO of A | (A == B) << 30, AO of B, block offset lo, hi)
 };

@@ -30,14 +30,25 @@ __global__ void __launch_bounds__(128) k_digest(DevBasis b, DevPairsExt pr, cons
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntask) return;
   const int2 tk = tasks[t];
-  const int A = __ldg(pr.p.A + tk.x), B = __ldg(pr.p.B + tk.x);
-  const int C = __ldg(pr.p.A + tk.y), Dd = __ldg(pr.p.B + tk.y);
-  const long long o = dev_blk(b, A);  // the four shells share one molecule
-  const int oa = __ldg(b.sh_ao + A), ob = __ldg(b.sh_ao + B), oc = __ldg(b.sh_ao + C), od = __ldg(b.sh_ao + Dd);
+  int oa, ob, oc, od;
+  long long o;  // the four shells share one molecule block
+  bool sab, scd;
+  if (pr.p.ao4) {  // one 16-byte load per pair instead of the shell tables
+    const int4 pb = __ldg(pr.p.ao4 + tk.x), pk = __ldg(pr.p.ao4 + tk.y);
+    oa = pb.x & 0x3FFFFFFF; ob = pb.y; oc = pk.x & 0x3FFFFFFF; od = pk.y;
+    sab = (pb.x >> 30) & 1; scd = (pk.x >> 30) & 1;
+    o = (long long)(unsigned)pb.z | ((long long)pb.w << 32);
+  } else {
+    const int A = __ldg(pr.p.A + tk.x), B = __ldg(pr.p.B + tk.x);
+    const int C = __ldg(pr.p.A + tk.y), Dd = __ldg(pr.p.B + tk.y);
+    o = dev_blk(b, A);
+    oa = __ldg(b.sh_ao + A); ob = __ldg(b.sh_ao + B); oc = __ldg(b.sh_ao + C); od = __ldg(b.sh_ao + Dd);
+    sab = A == B; scd = C == Dd;
+  }
   const int n = b.ld;
   D += o;
   G += o;
-  const double deg = (A == B ? 1.0 : 2.0) * (C == Dd ? 1.0 : 2.0) * (tk.x == tk.y ? 1.0 : 2.0);
+  const double deg = (sab ? 1.0 : 2.0) * (scd ? 1.0 : 2.0) * (tk.x == tk.y ? 1.0 : 2.0);
   double Dab[NA][NB], Dcd[NC][ND], Dac[NA][NC], Dbd[NB][ND], Dad[NA][ND], Dbc[NB][NC];
   double gab[NA][NB], gcd[NC][ND], gac[NA][NC], gbd[NB][ND], gad[NA][ND], gbc[NB][NC];
 #pragma unroll

@@ -22,7 +22,7 @@
 //     (checked; K = 298 allows s <= 11).
 //  3. Every level has its own FP32 buffer; one pass combines them exactly in int64,
 //     acc = sum_L P_L 2^{beta (s+1-L)} (|acc| < 2^60), and writes
-//     C = acc 2^{eA + eB - beta (s+1)} (one int64->FP64 conversion per element).
+//     C = acc 2^{eA + eB - beta (s+1)} (acc rounded to FP64 with integer operations).
 // Dropped terms (p + q > s + 1) bound the relative error of an element by about
 // K 2^{-beta s} of (row max of A) * (column max of B).
 //
@@ -100,7 +100,22 @@ __device__ __forceinline__ long long oz_out(bool roleA, long long v1, long long 
 }
 
 // Vectors contiguous (s0 == 1): one thread per vector; each k is one coalesced row of
-// consecutive vectors; the digit pass re-reads the column from L2.
+// consecutive vectors.  Two streaming passes: k_oz_vmax_v writes every vector's
+// exponent, then k_oz_split_v writes the digits.
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_vmax_v(const double* __restrict__ src, long long n1,
+                                                          long long s1, long long n0, int K, long long ks,
+                                                          int* __restrict__ exps) {
+  const long long chunks = (n0 + OZ_THREADS - 1) / OZ_THREADS;
+  const long long v1 = blockIdx.x / chunks;
+  const long long v0 = (blockIdx.x % chunks) * OZ_THREADS + threadIdx.x;
+  if (v1 >= n1 || v0 >= n0) return;
+  const double* x = src + v1 * s1 + v0;
+  unsigned long long m = 0;
+#pragma unroll 16
+  for (int k = 0; k < K; ++k) m = max(m, oz_absbits(__ldg(x + (long long)k * ks)));
+  exps[v1 * n0 + v0] = (int)(m >> 52);   // exponent field of the max (converted below)
+}
+
 template <int NS>
 __global__ void __launch_bounds__(OZ_THREADS) k_oz_split_v(const double* __restrict__ src, long long n1,
                                                            long long s1, long long n0, int K, long long ks,
@@ -111,10 +126,7 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_split_v(const double* __restr
   const long long v0 = (blockIdx.x % chunks) * OZ_THREADS + threadIdx.x;
   if (v1 >= n1 || v0 >= n0) return;
   const double* x = src + v1 * s1 + v0;
-  unsigned long long m = 0;
-#pragma unroll 8
-  for (int k = 0; k < K; ++k) m = max(m, oz_absbits(__ldg(x + (long long)k * ks)));
-  const int emax = (int)(m >> 52);
+  const int emax = exps[v1 * n0 + v0];
   exps[v1 * n0 + v0] = emax ? emax - 1022 : 0;
 #pragma unroll 4
   for (int k = 0; k < K; ++k) {
@@ -150,6 +162,29 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_split_k(const double* __restr
   }
 }
 
+// acc 2^e as a double, rounded to nearest even like an int64 -> FP64 conversion, built
+// with integer operations only (64-bit conversions run on the FP64 pipe); results
+// below the normal range are flushed to 0 (far under any tolerance here).
+__device__ __forceinline__ double oz_ll_scaled(long long acc, int e) {
+  if (acc == 0) return 0.0;
+  const unsigned long long sign = acc < 0 ? 1ull : 0ull;
+  unsigned long long mag = sign ? (unsigned long long)(-acc) : (unsigned long long)acc;
+  int msb = 63 - __clzll((long long)mag);
+  unsigned long long mant;
+  if (msb <= 52) {
+    mant = mag << (52 - msb);
+  } else {
+    const int sh = msb - 52;
+    mant = mag >> sh;
+    const unsigned long long rem = mag & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+    if (mant >> 53) { mant >>= 1; ++msb; }
+  }
+  const int ef = msb + 1023 + e;
+  if (ef <= 0) return 0.0;
+  return __longlong_as_double((long long)((sign << 63) | ((unsigned long long)ef << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
 // C[b][m][n] (+)= (sum_L P_L[b][m][n] 2^{beta (s+1-L)}) 2^{eA[bA][m] + eB[bB][n] - beta (s+1)}
 // One CTA per row r = b * M + m and chunk of 4 * OZ_THREADS columns.
 #define OZ_COMBINE_COLS (4 * OZ_THREADS)
@@ -171,18 +206,12 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_combine(const float* __restri
   for (int j = 0; j < 4; ++j) {
     const int n = c0 + j * OZ_THREADS + threadIdx.x;
     if (n >= N) break;
+    // level sums are integers below 2^24: FP32 -> int32 conversions, int64 shifts
     long long acc = 0;
     for (int L = 2; L <= nslice + 1; ++L)
-      acc += __float2ll_rn(__ldg(Pr + (long long)(L - 2) * pstride + n)) << (OZ_BETA * (nslice + 1 - L));
+      acc += (long long)__float2int_rn(__ldg(Pr + (long long)(L - 2) * pstride + n)) << (OZ_BETA * (nslice + 1 - L));
     const int e = ea + __ldg(eb + n);
-    double v = 0.0;
-    if (acc != 0) {
-      // exact power-of-two scaling by adding to the exponent field (no FP64 multiply)
-      long long bits = __double_as_longlong(__ll2double_rn(acc));
-      const int ef = (int)((bits >> 52) & 0x7FF) + e;
-      if (ef <= 0) v = 0.0;  // below the normal range: far under any tolerance here
-      else { bits = (bits & ~(0x7FFll << 52)) | ((long long)ef << 52); v = __longlong_as_double(bits); }
-    }
+    const double v = oz_ll_scaled(acc, e);
     Cr[n] = assign ? v : Cr[n] + v;
   }
 }
@@ -223,6 +252,7 @@ static void oz_launch_split(const double* src, long long nb, long long sb, long 
                                                                                   out, ex);
   } else {
     const long long chunks = (nv0 + OZ_THREADS - 1) / OZ_THREADS;
+    k_oz_vmax_v<<<(unsigned)(nb * chunks), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, K, sk, ex);
     k_oz_split_v<NS><<<(unsigned)(nb * chunks), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, K, sk, roleA, out, ex);
   }
 }

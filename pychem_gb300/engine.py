@@ -169,12 +169,13 @@ class GpuEngine:
                        PA=torch.empty(tot * 3, dtype=torch.float64, device=dv),
                        K=torch.empty(tot, dtype=torch.float64, device=dv),
                        Kf=torch.empty(tot, dtype=torch.float32, device=dv),
-                       oo2z=torch.empty(tot, dtype=torch.float64, device=dv))
+                       oo2z=torch.empty(tot, dtype=torch.float64, device=dv),
+                       ao4=torch.empty(self.npair * 4, dtype=torch.int32, device=dv))
         p = self.pd
         t = PairsT()
         t.npair = self.npair; t.npp = tot
         for k, f in (("A", "A"), ("B", "B"), ("ppoff", "ppoff"), ("npp", "npp_of"), ("AB", "AB"), ("zeta", "zeta"),
-                     ("P", "P"), ("PA", "PA"), ("K", "K"), ("oo2z", "oo2z"), ("Kf", "Kf")):
+                     ("P", "P"), ("PA", "PA"), ("K", "K"), ("oo2z", "oo2z"), ("Kf", "Kf"), ("ao4", "ao4")):
             setattr(t, f, p[k].data_ptr())
         self.pairs_t = t
         # pair kinds ordered by (pair class, nA, nB)
@@ -187,11 +188,14 @@ class GpuEngine:
         self.compute_pair_data()
 
     def compute_pair_data(self):
-        """Primitive-pair data from the device-resident shells (one kernel)."""
+        """Primitive-pair data and the per-pair AO table from the device-resident
+        shells (two kernels)."""
         p = self.pd
         _lib.call("pcg_pair_data", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ppoff"]),
                   _ptr(p["AB"]), _ptr(p["zeta"]), _ptr(p["P"]), _ptr(p["PA"]), _ptr(p["K"]), _ptr(p["Kf"]),
                   _ptr(p["oo2z"]), _stream())
+        _lib.call("pcg_pair_ao", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ao4"]),
+                  _stream())
 
     # ---------------------------------------------------------------------------------
     def one_electron(self):

@@ -2,9 +2,11 @@
 
     python -m pychem_gb300.profile_case --case water16 --phase eri [--repeat 2]
 
-cases:  water16 ((H2O)16 / 6-31G, 208 AO), water4 ((H2O)4 / 6-31G), alkane12
-        (C12H26 / cc-pVDZ, 298 AO)
-phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2)
+cases:  water16 ((H2O)16 / 6-31G, 208 AO), water8 ((H2O)8, 104 AO), water4 ((H2O)4),
+        alkane12 (C12H26 / cc-pVDZ, 298 AO), ensemble (256 perturbed small molecules,
+        6-31G, batched), mlp (the learned-guess network on 65,536 pairs)
+phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2);
+        for mlp: train (forward, loss, backward, Adam)
 """
 import argparse
 import time
@@ -18,6 +20,7 @@ from .scf import rhf, rmp2
 
 CASES = {
     "water16": lambda: Molecule(W.water_cluster(), "6-31G"),
+    "water8": lambda: Molecule(W.water_cluster(nx=2, ny=2, nz=2), "6-31G"),
     "water4": lambda: Molecule(W.water_cluster(nx=2, ny=2, nz=1), "6-31G"),
     "alkane12": lambda: Molecule(W.alkane(12), "cc-pVDZ"),
 }
@@ -25,11 +28,15 @@ CASES = {
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="water16", choices=sorted(CASES))
-    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2"])
+    ap.add_argument("--case", default="water16", choices=sorted(CASES) + ["ensemble", "mlp"])
+    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
+    if args.case == "ensemble":
+        return ensemble_case(args)
+    if args.case == "mlp":
+        return mlp_case(args)
     mol = CASES[args.case]()
     eng = GpuEngine(mol, precision=args.precision)
     eng.one_electron(); eng.schwarz(); eng.build_tasks(); eng.compute_eris()
@@ -50,6 +57,40 @@ def main():
     print("%s %s %s: %.4f s per repeat, %d quartets" % (args.case, args.phase, args.precision,
                                                          (time.perf_counter() - t0) / args.repeat,
                                                          eng.stats["quartets"]))
+
+
+def ensemble_case(args):
+    from .ensemble import EnsembleEngine, rhf_batched
+    mols = [Molecule(c, "6-31G") for c in W.ensemble(n=256, seed=2026)]
+    eng = EnsembleEngine(mols, precision=args.precision).prepare()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.repeat):
+        if args.phase == "eri":
+            eng.compute_eris()
+        else:
+            r = rhf_batched(eng)
+    torch.cuda.synchronize()
+    print("ensemble %s: %.4f s per repeat, %d molecules" % (args.phase, (time.perf_counter() - t0) / args.repeat,
+                                                           eng.B))
+
+
+def mlp_case(args):
+    from .learned.blocks import NFEAT, NPARAM
+    from .learned.mlp import PairMLP
+    net = PairMLP(seed=0)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    X = torch.randn(65536, NFEAT, device="cuda", generator=g)
+    T = torch.randn(65536, NPARAM, device="cuda", generator=g)
+    M = torch.ones_like(T)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.repeat):
+        Y, cache = net.forward(X, keep=True)
+        loss, dY = net.loss_grad(Y, T, M)
+        net.adam(net.backward(dY, cache), 1e-3)
+    torch.cuda.synchronize()
+    print("mlp train step: %.4f s per repeat" % ((time.perf_counter() - t0) / args.repeat))
 
 
 if __name__ == "__main__":
