@@ -137,6 +137,61 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_split_v(const double* __restr
   }
 }
 
+// The same two passes with 4 consecutive vectors per thread (32-byte loads, 8-byte
+// digit stores): used for role B when n0, s1 and ks are multiples of 4 and src is
+// 32-byte aligned, so a CTA reads 8 KB of one row per k.
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_vmax_v4(const double* __restrict__ src, long long n1,
+                                                           long long s1, long long n0, int K, long long ks,
+                                                           int* __restrict__ exps) {
+  const long long chunks = (n0 + 4 * OZ_THREADS - 1) / (4 * OZ_THREADS);
+  const long long v1 = blockIdx.x / chunks;
+  const long long v0 = ((blockIdx.x % chunks) * OZ_THREADS + threadIdx.x) * 4;
+  if (v1 >= n1 || v0 >= n0) return;
+  const double* x = src + v1 * s1 + v0;
+  unsigned long long m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+#pragma unroll 8
+  for (int k = 0; k < K; ++k) {
+    const double2 qa = __ldg((const double2*)(x + (long long)k * ks));
+    const double2 qb = __ldg((const double2*)(x + (long long)k * ks) + 1);
+    m0 = max(m0, oz_absbits(qa.x)); m1 = max(m1, oz_absbits(qa.y));
+    m2 = max(m2, oz_absbits(qb.x)); m3 = max(m3, oz_absbits(qb.y));
+  }
+  *(int4*)(exps + v1 * n0 + v0) = make_int4((int)(m0 >> 52), (int)(m1 >> 52), (int)(m2 >> 52), (int)(m3 >> 52));
+}
+
+template <int NS>
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_split_v4(const double* __restrict__ src, long long n1,
+                                                            long long s1, long long n0, int K, long long ks,
+                                                            __nv_bfloat16* __restrict__ out, int* __restrict__ exps) {
+  const long long chunks = (n0 + 4 * OZ_THREADS - 1) / (4 * OZ_THREADS);
+  const long long v1 = blockIdx.x / chunks;
+  const long long v0 = ((blockIdx.x % chunks) * OZ_THREADS + threadIdx.x) * 4;
+  if (v1 >= n1 || v0 >= n0) return;
+  const double* x = src + v1 * s1 + v0;
+  int4 em = *(const int4*)(exps + v1 * n0 + v0);
+  *(int4*)(exps + v1 * n0 + v0) = make_int4(em.x ? em.x - 1022 : 0, em.y ? em.y - 1022 : 0, em.z ? em.z - 1022 : 0,
+                                            em.w ? em.w - 1022 : 0);
+#pragma unroll 2
+  for (int k = 0; k < K; ++k) {
+    const double2 qa = __ldg((const double2*)(x + (long long)k * ks));
+    const double2 qb = __ldg((const double2*)(x + (long long)k * ks) + 1);
+    int d0[NS], d1[NS], d2[NS], d3[NS];
+    oz_digits<NS>(qa.x, em.x, d0);
+    oz_digits<NS>(qa.y, em.y, d1);
+    oz_digits<NS>(qb.x, em.z, d2);
+    oz_digits<NS>(qb.y, em.w, d3);
+#pragma unroll
+    for (int p = 1; p <= NS; ++p) {
+      __nv_bfloat162 lo = __halves2bfloat162(__int2bfloat16_rn(d0[p - 1]), __int2bfloat16_rn(d1[p - 1]));
+      __nv_bfloat162 hi = __halves2bfloat162(__int2bfloat16_rn(d2[p - 1]), __int2bfloat16_rn(d3[p - 1]));
+      uint2 w;
+      w.x = *(unsigned*)&lo;
+      w.y = *(unsigned*)&hi;
+      *(uint2*)(out + ((v1 * NS + NS - p) * (long long)K + k) * n0 + v0) = w;
+    }
+  }
+}
+
 // k contiguous (ks == 1): one warp per vector, lanes over k.
 template <int NS>
 __global__ void __launch_bounds__(OZ_THREADS) k_oz_split_k(const double* __restrict__ src, long long n1,
@@ -216,6 +271,43 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_combine(const float* __restri
   }
 }
 
+// The same with 4 consecutive columns per thread (16-byte level loads and stores)
+// when N and sCb are multiples of 4.
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_combine4(const float* __restrict__ P, long long pstride,
+                                                            int nslice, double* __restrict__ C, long long rows, int M,
+                                                            int N, long long sCb, const int* __restrict__ eA,
+                                                            int a_batched, const int* __restrict__ eB, int b_batched,
+                                                            int assign) {
+  const long long nch = (N + OZ_COMBINE_COLS - 1) / OZ_COMBINE_COLS;
+  const long long r = blockIdx.x / nch;
+  if (r >= rows) return;
+  const int n = (int)(blockIdx.x % nch) * OZ_COMBINE_COLS + 4 * threadIdx.x;
+  if (n >= N) return;
+  const long long b = r / M;
+  const int m = (int)(r % M);
+  const int ea = eA[(a_batched ? b * M : 0) + m] - OZ_BETA * (nslice + 1);
+  const int4 eb = __ldg((const int4*)(eB + (b_batched ? b * N : 0) + n));
+  const float* Pr = P + r * N + n;
+  long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  for (int L = 2; L <= nslice + 1; ++L) {
+    const float4 q = __ldg((const float4*)(Pr + (long long)(L - 2) * pstride));
+    const int sh = OZ_BETA * (nslice + 1 - L);
+    a0 += (long long)__float2int_rn(q.x) << sh;
+    a1 += (long long)__float2int_rn(q.y) << sh;
+    a2 += (long long)__float2int_rn(q.z) << sh;
+    a3 += (long long)__float2int_rn(q.w) << sh;
+  }
+  double2 v0 = make_double2(oz_ll_scaled(a0, ea + eb.x), oz_ll_scaled(a1, ea + eb.y));
+  double2 v1 = make_double2(oz_ll_scaled(a2, ea + eb.z), oz_ll_scaled(a3, ea + eb.w));
+  double2* c = (double2*)(C + b * sCb + (long long)m * N + n);
+  if (!assign) {
+    const double2 o0 = c[0], o1 = c[1];
+    v0.x += o0.x; v0.y += o0.y; v1.x += o1.x; v1.y += o1.y;
+  }
+  c[0] = v0;
+  c[1] = v1;
+}
+
 static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 struct OzLayout {
@@ -250,6 +342,10 @@ static void oz_launch_split(const double* src, long long nb, long long sb, long 
     const long long per = OZ_THREADS / 32;
     k_oz_split_k<NS><<<(unsigned)((nb * nv0 + per - 1) / per), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, sv0, K, roleA,
                                                                                   out, ex);
+  } else if (!roleA && nv0 % 4 == 0 && (nb == 1 || sb % 4 == 0) && sk % 4 == 0 && ((size_t)src & 31) == 0) {
+    const long long chunks = (nv0 + 4 * OZ_THREADS - 1) / (4 * OZ_THREADS);
+    k_oz_vmax_v4<<<(unsigned)(nb * chunks), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, K, sk, ex);
+    k_oz_split_v4<NS><<<(unsigned)(nb * chunks), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, K, sk, out, ex);
   } else {
     const long long chunks = (nv0 + OZ_THREADS - 1) / OZ_THREADS;
     k_oz_vmax_v<<<(unsigned)(nb * chunks), OZ_THREADS, 0, s>>>(src, nb, sb, nv0, K, sk, ex);
@@ -336,8 +432,12 @@ extern "C" int pcg_ozaki_gemm(const pcg_gemm_desc_t* d, const double* A, const d
   }
   const long long rows = (long long)d->batch * d->M;
   const long long nch = (d->N + OZ_COMBINE_COLS - 1) / OZ_COMBINE_COLS;
-  k_oz_combine<<<(unsigned)(rows * nch), OZ_THREADS, 0, s>>>(P, L.pstride, nslice, C, rows, d->M, d->N, d->sCb, eA,
-                                                              d->sAb ? 1 : 0, eB, d->sBb ? 1 : 0, accumulate ? 0 : 1);
+  if (d->N % 4 == 0 && d->sCb % 4 == 0 && ((size_t)C & 31) == 0)
+    k_oz_combine4<<<(unsigned)(rows * nch), OZ_THREADS, 0, s>>>(P, L.pstride, nslice, C, rows, d->M, d->N, d->sCb, eA,
+                                                                 d->sAb ? 1 : 0, eB, d->sBb ? 1 : 0, accumulate ? 0 : 1);
+  else
+    k_oz_combine<<<(unsigned)(rows * nch), OZ_THREADS, 0, s>>>(P, L.pstride, nslice, C, rows, d->M, d->N, d->sCb, eA,
+                                                                d->sAb ? 1 : 0, eB, d->sBb ? 1 : 0, accumulate ? 0 : 1);
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;
 }

@@ -19,6 +19,9 @@ from . import _lib
 
 FP64_JACOBI_MAX_N = 136
 
+# counts of eigh calls by route (exact library solve, refinement, refinement rejected)
+stats = {"exact": 0, "refined": 0, "fallback": 0}
+
 
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -132,16 +135,30 @@ def eigh(A, X_prev=None, refine_steps=2, exact=True, check_tol=1e-10, nocc=None)
             return _sort(w, X_prev @ V)
         return _sort(*jacobi(A))
     if exact or X_prev is None:
+        stats["exact"] += 1
         return torch.linalg.eigh(A)
     I = torch.eye(n, dtype=torch.float64, device=A.device)
     if nocc is not None:
-        # SCF iterations: only the occupied-space projector matters
-        w, X = refine_projector(A, X_prev, nocc, steps=refine_steps)
-        orth = (X.transpose(-1, -2) @ X - I).abs().amax()
-        gap = w[nocc:].min() - w[:nocc].max()
-        chk = torch.stack([orth, -gap]).cpu()
-        if float(chk[0]) > check_tol or float(chk[1]) >= 0.0:
+        # SCF iterations: only the occupied-space projector matters.  Refine in rounds
+        # of refine_steps steps until the vectors are orthonormal, the occupied block is
+        # decoupled (max |(X^T A X)_ov| <= check_tol |A|) and gapped; after three rounds
+        # fall back to the exact solver.
+        X = X_prev
+        scale = float(A.abs().amax())
+        ok = False
+        for _ in range(3):
+            w, X = refine_projector(A, X, nocc, steps=refine_steps)
+            orth = (X.transpose(-1, -2) @ X - I).abs().amax()
+            ov = (X[:, :nocc].transpose(-1, -2) @ (A @ X[:, nocc:])).abs().amax()
+            gap = w[nocc:].min() - w[:nocc].max()
+            chk = torch.stack([orth, ov, -gap]).cpu()
+            if float(chk[0]) <= check_tol and float(chk[1]) <= check_tol * max(scale, 1.0) and float(chk[2]) < 0.0:
+                ok = True
+                break
+        if not ok:
+            stats["fallback"] += 1
             return torch.linalg.eigh(A)
+        stats["refined"] += 1
         wo, io = torch.sort(w[:nocc])
         wv, iv = torch.sort(w[nocc:])
         return torch.cat([wo, wv]), torch.cat([X[:, :nocc][:, io], X[:, nocc:][:, iv]], dim=1)

@@ -71,11 +71,16 @@ class SCFResult(dict):
 
 
 def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=1, D0=None, record=False,
-        guess="sad"):
+        guess="sad", exact_iters=3):
     """Restricted Hartree-Fock on a prepared GpuEngine.  Returns SCFResult with
     E (total), E_elec, C, eps, D (alpha density), iterations, converged.
     guess: "sad" (superposition of atomic densities, default), "core" (upstream's
-    core-Hamiltonian guess), or an explicit alpha density D0."""
+    core-Hamiltonian guess), or an explicit alpha density D0.
+
+    Fock matrices are kept in the orthonormal basis, F' = X^T F X; the DIIS residual
+    is D'F' - F'D' (= X^T (S D F - F D S) X for D = X D' X^T) and DIIS extrapolates F'.
+    The first exact_iters iterations diagonalise exactly; later ones refine the
+    previous eigenvectors (checked, with fallback to the exact solver)."""
     mol = engine.mol
     nocc = mol.NAlphaElectrons
     if mol.NAlphaElectrons != mol.NBetaElectrons:
@@ -87,8 +92,8 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
     Xt = X.T.contiguous()
     state = {"Q": None}
 
-    def diagonalise(F, exact=False):
-        e, Q = eigen.eigh(Xt @ F @ X, X_prev=state["Q"], refine_steps=2, exact=exact, nocc=nocc)
+    def diagonalise(Fp, exact=False):
+        e, Q = eigen.eigh(Fp, X_prev=state["Q"], refine_steps=2, exact=exact, nocc=nocc)
         state["Q"] = Q
         return e, X @ Q
 
@@ -98,8 +103,9 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
         from .guess import sad_density
         D = sad_density(mol, device=dev)
     else:
-        eps, C = diagonalise(H)
+        eps, C = diagonalise(Xt @ H @ X)
         D = C[:, :nocc] @ C[:, :nocc].T
+    Dp = Xt @ S @ D @ S @ X      # orthonormal-basis density
     n = engine.nbf
     F = torch.empty(n, n, dtype=torch.float64, device=dev)
     G = torch.empty(n, n, dtype=torch.float64, device=dev)
@@ -112,7 +118,12 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
     for it in range(1, max_iter + 1):
         engine.fock(D, out=F, G=G)
         use_diis = it > diis_start
-        R = Xt @ (S @ D @ F - F @ D @ S) @ X if use_diis else None
+        Fp = Xt @ F @ X
+        if use_diis:
+            P = Dp @ Fp
+            R = P - P.T
+        else:
+            R = None
         # one device->host read per iteration: energy, density change, new DIIS row
         vals = [torch.sum(D * (H + F)).reshape(1)]
         vals.append(torch.sqrt(torch.mean((D - D_old) ** 2)).reshape(1) if D_old is not None
@@ -131,7 +142,7 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                 converged = True
                 break
         E_old, D_old = E, D
-        Fx = F
+        Fx = Fp
         if use_diis:
             row = host[2:]
             m = len(resids) + 1
@@ -139,7 +150,7 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
             Bn[:m - 1, :m - 1] = Bmat
             Bn[m - 1, :] = row
             Bn[:, m - 1] = row
-            focks.append(F.clone())
+            focks.append(Fp)
             resids.append(R)
             Bmat = Bn
             if len(focks) > diis_size:
@@ -149,13 +160,14 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                 c = diis_coefficients(Bmat)
                 cw = torch.tensor(c, dtype=torch.float64, device=dev)
                 Fx = torch.einsum("k,kij->ij", cw, torch.stack(focks))
-        # first iterations move the orbitals a lot: exact solver; afterwards refine the
-        # previous eigenvectors (checked, with fallback)
-        eps, C = diagonalise(Fx, exact=it <= 3)
-        D = C[:, :nocc] @ C[:, :nocc].T
+        eps, C = diagonalise(Fx, exact=it <= exact_iters)
+        Co = C[:, :nocc]
+        D = Co @ Co.T
+        Qo = state["Q"][:, :nocc]
+        Dp = Qo @ Qo.T
     # orbitals of the final Fock matrix, exact (including inside near-degenerate
     # clusters) for MP2's denominators
-    eps, C = diagonalise(F, exact=True)
+    eps, C = diagonalise(Xt @ F @ X, exact=True)
     return SCFResult(E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=C, eps=eps, D=D, F=F, iterations=it,
                      converged=converged, history=history, fock_builds=it)
 
