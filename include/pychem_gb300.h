@@ -149,6 +149,10 @@ typedef struct {
    * of B, low and high 32 bits of the molecule block offset), filled by pcg_pair_ao;
    * the Fock digestion reads it instead of the shell tables. */
   const int *ao4;
+  /* Optional (NULL allowed): per primitive pair 8 floats (zeta, P-A xyz, 1/(2 zeta), K,
+   * 0, 0), filled by pcg_pair_data_f32; the FP32 ERI kernels read it instead of
+   * converting the double arrays. */
+  const float *pf8;
 } pcg_pairs_t;
 
 /* Primitive-pair data for npair pairs (replaces the per-pair ShellPair set-up,
@@ -156,6 +160,11 @@ typedef struct {
 int pcg_pair_data(const pcg_basis_t *basis, int npair, const int *A, const int *B,
                   const int *ppoff, double *AB, double *zeta, double *P, double *PA, double *K,
                   float *Kf, double *oo2z, void *stream);
+
+/* The packed FP32 primitive-pair table pcg_pairs_t.pf8 (npp x 8 floats) from the
+ * double arrays of pcg_pair_data. */
+int pcg_pair_data_f32(int npp, const double *zeta, const double *PA, const double *oo2z, const float *Kf,
+                      float *pf8, void *stream);
 
 /* The per-pair AO table pcg_pairs_t.ao4 (npair x 4 ints) from the shell tables. */
 int pcg_pair_ao(const pcg_basis_t *basis, int npair, const int *A, const int *B, int *ao4, void *stream);

@@ -38,7 +38,8 @@ class GemmDescT(ctypes.Structure):
 class PairsT(ctypes.Structure):
     _fields_ = [("npair", c_int), ("npp", c_int), ("A", c_void_p), ("B", c_void_p), ("ppoff", c_void_p),
                 ("npp_of", c_void_p), ("AB", c_void_p), ("zeta", c_void_p), ("P", c_void_p), ("PA", c_void_p),
-                ("K", c_void_p), ("oo2z", c_void_p), ("Kf", c_void_p), ("ao4", c_void_p)]
+                ("K", c_void_p), ("oo2z", c_void_p), ("Kf", c_void_p), ("ao4", c_void_p),
+                ("pf8", c_void_p)]
 
 
 # name -> argtypes (all return int status unless listed in _RESTYPES)
@@ -58,6 +59,7 @@ _SIGS = {
     "pcg_one_electron_kinetic": [P_DBL, PP_DBL, P_DBL] + [c_int] * 5,
     "pcg_one_electron_contract": [P_DBL, P_DBL, P_DBL] + [c_int] * 4,
     "pcg_pair_data": [ctypes.POINTER(BasisT), c_int] + [c_void_p] * 10 + [c_void_p],
+    "pcg_pair_data_f32": [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "pcg_pair_ao": [ctypes.POINTER(BasisT), c_int, c_void_p, c_void_p, c_void_p, c_void_p],
     "pcg_one_electron": [ctypes.POINTER(BasisT), c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "pcg_eri_class_id": [c_int] * 4,
@@ -89,7 +91,7 @@ _SIGS = {
                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
 }
 # entry points that launch exactly one kernel of this library per call
-LAUNCHERS = {"pcg_pair_data", "pcg_pair_ao", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
+LAUNCHERS = {"pcg_pair_data", "pcg_pair_data_f32", "pcg_pair_ao", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
              "pcg_digest_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh", "pcg_mlp_gemm", "pcg_mlp_dsilu",
              "pcg_mlp_colsum", "pcg_mlp_mse", "pcg_mlp_adam",
              "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",

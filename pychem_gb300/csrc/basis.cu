@@ -117,6 +117,23 @@ int pcg_launch_pair_data(const DevBasis& b, int npair, const int* pA, const int*
   return PCG_OK;
 }
 
+__global__ void k_pair_data_f32(int npp, const double* __restrict__ zeta, const double* __restrict__ PA,
+                                const double* __restrict__ oo2z, const float* __restrict__ Kf,
+                                float4* __restrict__ pf8) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npp) return;
+  pf8[2 * k] = make_float4((float)zeta[k], (float)PA[3 * k], (float)PA[3 * k + 1], (float)PA[3 * k + 2]);
+  pf8[2 * k + 1] = make_float4((float)oo2z[k], Kf[k], 0.0f, 0.0f);
+}
+
+int pcg_launch_pair_data_f32(int npp, const double* zeta, const double* PA, const double* oo2z, const float* Kf,
+                             float* pf8, cudaStream_t s) {
+  if (npp <= 0) return PCG_OK;
+  k_pair_data_f32<<<(npp + 255) / 256, 256, 0, s>>>(npp, zeta, PA, oo2z, Kf, (float4*)pf8);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
 __global__ void k_pair_ao(DevBasis b, int npair, const int* __restrict__ pA, const int* __restrict__ pB,
                           int4* __restrict__ ao4) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;

@@ -36,6 +36,7 @@ static DevPairsExt to_dev(const pcg_pairs_t* p) {
   d.p.A = p->A; d.p.B = p->B; d.p.ppoff = p->ppoff; d.p.npp_of = p->npp_of;
   d.p.AB = p->AB; d.p.zeta = p->zeta; d.p.P = p->P; d.p.PA = p->PA; d.p.K = p->K; d.p.Kf = p->Kf;
   d.p.ao4 = (const int4*)p->ao4;
+  d.p.pf8 = (const float4*)p->pf8;
   d.oo2z = p->oo2z;
   return d;
 }
@@ -57,6 +58,15 @@ int pcg_pair_data(const pcg_basis_t* basis, int npair, const int* A, const int* 
   if (!basis || npair < 0) { pcg_set_error("pcg_pair_data: bad arguments"); return PCG_ERR_ARG; }
   return pcg_launch_pair_data(to_dev(basis), npair, A, B, ppoff, AB, zeta, P, PA, K, Kf, oo2z,
                               (cudaStream_t)stream);
+}
+
+int pcg_pair_data_f32(int npp, const double* zeta, const double* PA, const double* oo2z, const float* Kf, float* pf8,
+                      void* stream) {
+  if (npp < 0 || (npp > 0 && (!zeta || !PA || !oo2z || !Kf || !pf8))) {
+    pcg_set_error("pcg_pair_data_f32: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  return pcg_launch_pair_data_f32(npp, zeta, PA, oo2z, Kf, pf8, (cudaStream_t)stream);
 }
 
 int pcg_pair_ao(const pcg_basis_t* basis, int npair, const int* A, const int* B, int* ao4, void* stream) {

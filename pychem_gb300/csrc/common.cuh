@@ -67,8 +67,11 @@ __device__ __forceinline__ double nr_rcp(double x) {
 template <int L>
 __device__ __forceinline__ void boys_eval(const BoysTable& bt, double T, double* F) {
   if (T < BOYS_TMAX) {
-    const int p = __float2int_rn((float)(T * BOYS_INV_H));
-    const double d = (double)p * (1.0 / BOYS_INV_H) - T;  // -(T - T_p)
+    // nearest grid point without conversions: adding 1.5 * 2^52 rounds T * 16 to an
+    // integer held in the low mantissa bits
+    const double r = fma(T, (double)BOYS_INV_H, 6755399441055744.0);
+    const int p = __double2loint(r);
+    const double d = (r - 6755399441055744.0) * (1.0 / BOYS_INV_H) - T;  // -(T - T_p)
     const double* row = bt.c + ((size_t)p * BOYS_M + L) * BOYS_K;
     double f = __ldg(row + BOYS_K - 1);
 #pragma unroll
@@ -197,4 +200,5 @@ struct DevPairs {
   const double* K;
   const float* Kf;
   const int4* ao4;    // optional: (AO of A | (A == B) << 30, AO of B, block offset lo, hi)
+  const float4* pf8;  // optional: per primitive pair (zeta, PA xyz), (1/(2 zeta), K, 0, 0)
 };

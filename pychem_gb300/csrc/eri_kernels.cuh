@@ -77,6 +77,48 @@ __global__ void __launch_bounds__(128) k_eri_f(DevPairsExt pr, BoysTable bt, con
   float acc[C::NACC];
 #pragma unroll
   for (int k = 0; k < C::NACC; ++k) acc[k] = 0.0f;
+  if (pr.p.pf8) {
+    // packed FP32 pair table: P - Q = (P - A) - (Q - C) + (A - C), the shell-centre
+    // difference A - C formed once per quartet in double precision
+    const float ACx = (float)((__ldg(pr.p.P + 3 * i0) - __ldg(pr.p.PA + 3 * i0)) -
+                              (__ldg(pr.p.P + 3 * j0) - __ldg(pr.p.PA + 3 * j0)));
+    const float ACy = (float)((__ldg(pr.p.P + 3 * i0 + 1) - __ldg(pr.p.PA + 3 * i0 + 1)) -
+                              (__ldg(pr.p.P + 3 * j0 + 1) - __ldg(pr.p.PA + 3 * j0 + 1)));
+    const float ACz = (float)((__ldg(pr.p.P + 3 * i0 + 2) - __ldg(pr.p.PA + 3 * i0 + 2)) -
+                              (__ldg(pr.p.P + 3 * j0 + 2) - __ldg(pr.p.PA + 3 * j0 + 2)));
+    for (int i = i0; i < i1; ++i) {
+      const float4 a0 = __ldg(pr.p.pf8 + 2 * i), a1 = __ldg(pr.p.pf8 + 2 * i + 1);
+      const float zeta = a0.x, Kp = a1.y;
+      PQf q;
+      q.PAx = a0.y; q.PAy = a0.z; q.PAz = a0.w;
+      q.oo2z = a1.x;
+      for (int j = j0; j < j1; ++j) {
+        const float4 b0 = __ldg(pr.p.pf8 + 2 * j), b1 = __ldg(pr.p.pf8 + 2 * j + 1);
+        const float eta = b0.x;
+        const float PQx = (q.PAx - b0.y) + ACx;
+        const float PQy = (q.PAy - b0.z) + ACy;
+        const float PQz = (q.PAz - b0.w) + ACz;
+        const float rs = rsqrtf(zeta + eta);
+        const float izpe = rs * rs;
+        const float rho = zeta * eta * izpe;
+        const float T = rho * fmaf(PQx, PQx, fmaf(PQy, PQy, PQz * PQz));
+        float F[C::L + 1];
+        boys_eval_f<C::L>(bt, T, F);
+        const float pre = Kp * b1.y * rs;
+#pragma unroll
+        for (int m = 0; m <= C::L; ++m) F[m] *= pre;
+        const float wp = -eta * izpe, wq = zeta * izpe;
+        q.WPx = wp * PQx; q.WPy = wp * PQy; q.WPz = wp * PQz;
+        q.WQx = wq * PQx; q.WQy = wq * PQy; q.WQz = wq * PQz;
+        q.QCx = b0.y; q.QCy = b0.z; q.QCz = b0.w;
+        q.oo2e = b1.x;
+        q.oo2ze = 0.5f * izpe;
+        q.rz = eta * izpe;
+        q.re = zeta * izpe;
+        C::prim(q, F, acc);
+      }
+    }
+  } else
   for (int i = i0; i < i1; ++i) {
     const double zd = __ldg(pr.p.zeta + i);
     const float zeta = (float)zd;

@@ -46,6 +46,7 @@ static DevPairsExt pairs_of(const pcg_pairs_t* p) {
   d.p.A = p->A; d.p.B = p->B; d.p.ppoff = p->ppoff; d.p.npp_of = p->npp_of;
   d.p.AB = p->AB; d.p.zeta = p->zeta; d.p.P = p->P; d.p.PA = p->PA; d.p.K = p->K; d.p.Kf = p->Kf;
   d.p.ao4 = (const int4*)p->ao4;
+  d.p.pf8 = (const float4*)p->pf8;
   d.oo2z = p->oo2z;
   return d;
 }

@@ -33,6 +33,8 @@ struct DevPairsExt {
 int pcg_launch_eri(int cls, const DevBasis& b, const DevPairsExt& pr, const BoysTable& bt, const int2* tasks,
                    int ntask, double* store, int precision, float fp32_below, const double* qpair,
                    cudaStream_t s);
+int pcg_launch_pair_data_f32(int npp, const double* zeta, const double* PA, const double* oo2z, const float* Kf,
+                             float* pf8, cudaStream_t s);
 int pcg_launch_pair_ao(const DevBasis& b, int npair, const int* pA, const int* pB, int* ao4, cudaStream_t s);
 int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                       const double* store, const double* D, double* G, cudaStream_t s);

@@ -170,12 +170,13 @@ class GpuEngine:
                        K=torch.empty(tot, dtype=torch.float64, device=dv),
                        Kf=torch.empty(tot, dtype=torch.float32, device=dv),
                        oo2z=torch.empty(tot, dtype=torch.float64, device=dv),
-                       ao4=torch.empty(self.npair * 4, dtype=torch.int32, device=dv))
+                       ao4=torch.empty(self.npair * 4, dtype=torch.int32, device=dv),
+                       pf8=torch.empty(tot * 8, dtype=torch.float32, device=dv))
         p = self.pd
         t = PairsT()
         t.npair = self.npair; t.npp = tot
         for k, f in (("A", "A"), ("B", "B"), ("ppoff", "ppoff"), ("npp", "npp_of"), ("AB", "AB"), ("zeta", "zeta"),
-                     ("P", "P"), ("PA", "PA"), ("K", "K"), ("oo2z", "oo2z"), ("Kf", "Kf"), ("ao4", "ao4")):
+                     ("P", "P"), ("PA", "PA"), ("K", "K"), ("oo2z", "oo2z"), ("Kf", "Kf"), ("ao4", "ao4"), ("pf8", "pf8")):
             setattr(t, f, p[k].data_ptr())
         self.pairs_t = t
         # pair kinds ordered by (pair class, nA, nB)
@@ -188,14 +189,16 @@ class GpuEngine:
         self.compute_pair_data()
 
     def compute_pair_data(self):
-        """Primitive-pair data and the per-pair AO table from the device-resident
-        shells (two kernels)."""
+        """Primitive-pair data, the per-pair AO table and the packed FP32 primitive-pair
+        table from the device-resident shells (three kernels)."""
         p = self.pd
         _lib.call("pcg_pair_data", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ppoff"]),
                   _ptr(p["AB"]), _ptr(p["zeta"]), _ptr(p["P"]), _ptr(p["PA"]), _ptr(p["K"]), _ptr(p["Kf"]),
                   _ptr(p["oo2z"]), _stream())
         _lib.call("pcg_pair_ao", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ao4"]),
                   _stream())
+        _lib.call("pcg_pair_data_f32", int(p["zeta"].numel()), _ptr(p["zeta"]), _ptr(p["PA"]), _ptr(p["oo2z"]),
+                  _ptr(p["Kf"]), _ptr(p["pf8"]), _stream())
 
     # ---------------------------------------------------------------------------------
     def one_electron(self):
