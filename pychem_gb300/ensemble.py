@@ -238,8 +238,9 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
     are restored on return).
 
     dense_fp32_until > 0 (mixed precision): while a molecule's DIIS residual has RMS
-    above this value its dense steps (X^T F X, residual, eigensolver, density) run in
-    FP32; below it, and for every iteration that can declare convergence, in FP64.
+    above this value (1e-4 is the tested setting) and for at most 8 iterations, its
+    dense steps (X^T F X, residual, eigensolver, density) run in FP32; after that, and
+    for every iteration that can declare convergence, in FP64.
     Fock builds, DIIS extrapolation and energies are FP64 throughout, so the converged
     state is the FP64 one.
 
@@ -349,21 +350,20 @@ def rhf_batched(eng, max_iter=64, e_tol=1e-10, d_tol=1e-8, diis_size=8, guess="s
                         eng.restrict(mask)
                         covered = len(act)
             E_old, D_old = E, D
-            # FP32 dense steps end once the residual is small (or after 16 iterations)
+            # FP32 dense steps end once the residual is small, or after 8 iterations:
+            # long FP32 phases (residual thresholds of 1e-5 and below) were seen to
+            # steer single molecules into a higher SCF solution
             rms = np.sqrt(np.maximum(host[:, -1], 0.0) / (n * n))
             n32 += p32
-            p32_new = p32 & (rms > dense_fp32_until) & (n32 < 16)
+            p32_new = p32 & (rms > dense_fp32_until) & (n32 < 8)
             switched = np.nonzero(p32 & ~p32_new)[0]
             p32 = p32_new
             if len(switched) and Q is not None:
-                # FP32-accurate eigenvectors start the FP64 steps: make them orthonormal
-                # to FP64 accuracy (two Newton-Schulz steps of the polar factor)
+                # the first FP64 step of a molecule starts from the identity (a full
+                # Jacobi solve) instead of its FP32 eigenvectors, whose orthogonality
+                # error would otherwise persist through X_prev
                 sw = torch.as_tensor(switched, device=dev)
-                Qs = Q.index_select(0, sw)
-                I = torch.eye(n, dtype=torch.float64, device=dev)
-                for _ in range(2):
-                    Qs = Qs @ (1.5 * I - 0.5 * Qs.transpose(-1, -2) @ Qs)
-                Q.index_copy_(0, sw, Qs)
+                Q.index_copy_(0, sw, torch.eye(n, dtype=torch.float64, device=dev).expand(len(switched), n, n))
             row = host[:, 2:]
             m = row.shape[1]
             Bn = np.zeros((len(act), m, m))
