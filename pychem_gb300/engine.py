@@ -32,7 +32,7 @@ def pair_class(la, lb):
     return la * (la + 1) // 2 + lb
 
 
-def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32):
+def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32, kind_work=None):
     """Screened canonical quartet plan (Methods/hartree_fock.py:241-312: the quartet
     loop, the Schwarz test Q_ab Q_cd > threshold, and the diagonal quartet that is
     always computed), with tensor operations on Q's device.
@@ -51,7 +51,10 @@ def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32):
     class and part ordered by (bra kind, ket kind, bra position) -- buckets of uniform
     primitive counts -- with bra pair ids, task offsets off (int64, rows + 1, starting
     at 0), first ket position qstart in ket_list (the pair ids in sorted order) and
-    the diagonal flag; row r covers tasks [off[r], off[r+1])."""
+    the diagonal flag; row r covers tasks [off[r], off[r+1]).  With kind_work (work
+    per pair of each kind, e.g. its primitive-pair count) the buckets run in
+    decreasing work per quartet, so a launch's heaviest CTAs start first and the light
+    ones fill its tail."""
     dev = Q.device
     nk = int(class_table.shape[0])
     o = torch.sort(-Q, stable=True).indices
@@ -65,7 +68,11 @@ def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32):
     first = torch.cumsum(ks + 1, 0) - (ks + 1)
     kk = torch.arange(pos.numel(), device=dev) - first[pos]
     kb = ks[pos]
-    ro = torch.sort((kb * nk + kk) * npair + pos).indices
+    key = (kb * nk + kk) * npair + pos
+    if kind_work is not None:
+        w = kind_work[kb] * kind_work[kk]
+        key = (int(w.max()) - w) * (nk * nk * npair) + key
+    ro = torch.sort(key).indices
     pos, kk, kb = pos[ro], kk[ro], kb[ro]
     qb = Qs[pos]
     key = kk * nmol + ms[pos]
@@ -251,9 +258,10 @@ class GpuEngine:
             for j in range(i + 1):
                 ct[i, j] = lib.pcg_eri_class_id(int(kl[i, 0]), int(kl[i, 1]), int(kl[j, 0]), int(kl[j, 1]))
         mol, nmol = self._pair_molecule()
+        work = torch.as_tensor([k[1] * k[2] for k in self.kinds], dtype=torch.int64, device=dev)
         plan, ket_list = plan_quartets(self.Q, torch.as_tensor(self.pair_kind, dtype=torch.int64, device=dev), mol,
                                        nmol, torch.as_tensor(ct, device=dev), float(self.threshold),
-                                       float(self.fp32_below))
+                                       float(self.fp32_below), kind_work=work)
         totals = torch.stack([x[3][-1] for x in plan]).cpu().tolist() if plan else []
         ket32 = ket_list.to(torch.int32)
         self.classes = {}

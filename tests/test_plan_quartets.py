@@ -35,7 +35,8 @@ def test_plan_matches_brute_force(trial):
     mol = torch.as_tensor(rng.integers(0, nmol, npair))
     ct = torch.as_tensor(rng.integers(0, 3, (nk, nk)))
     thr, thr32 = 1e-8, (1e-4 if trial % 2 else 0.0)
-    plan, ket = plan_quartets(Q, kind, mol, nmol, ct, thr, thr32)
+    work = torch.as_tensor(rng.integers(1, 5, nk)) if trial % 4 == 1 else None
+    plan, ket = plan_quartets(Q, kind, mol, nmol, ct, thr, thr32, kind_work=work)
     got, rows = _expand(plan, ket)
     order = ket.numpy()
     posn = np.empty(npair, dtype=np.int64)
@@ -52,7 +53,9 @@ def test_plan_matches_brute_force(trial):
             fp32 = screened and thr32 > 0 and not Qn[p] * Qn[q] > thr32
             want[(p, q)] = (int(ct[kn[p], kn[q]]), "32" if fp32 else "64")
     assert got == want
-    # within a class list the rows run in (bra kind, ket kind, bra position) order
+    # within a class list the rows run in (-work, bra kind, ket kind, bra position) order
+    wk = work.numpy() if work is not None else np.ones(nk, dtype=np.int64)
     for cls, part, bra, off, qs, dg in plan:
-        keyr = [(kn[int(b)], kn[order[int(s)]], posn[int(b)]) for b, s in zip(bra, qs)]
+        keyr = [(-wk[kn[int(b)]] * wk[kn[order[int(s)]]], kn[int(b)], kn[order[int(s)]], posn[int(b)])
+                for b, s in zip(bra, qs)]
         assert keyr == sorted(keyr)
