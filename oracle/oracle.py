@@ -19,6 +19,10 @@ import this module, always as the checker.  It restates the upstream algorithm:
   |dE| stop only); ``mode='consistent'`` (the default judge) takes the energy from the
   Fock built from the current density and stops on |dE| < 1e-10 and D-RMS < 1e-8.
 * MP2: closed-shell form of ``Methods/mp2.py:43-94`` (identical value for RHF).
+* Open shells: UHF and CUHF along ``Methods/hartree_fock.py:23-142`` with the per-spin
+  DIIS of ``Methods/hf_extensions/diis.py`` and the CUHF constraint of
+  ``hartree_fock.py:359-391`` (natural orbitals of S^1/2 (D_tot/2) S^1/2), and UMP2 as
+  ``Methods/mp2.py:43-101``; pinned by ``tests/test_oracle_open_shell.py``.
 """
 import ctypes
 import json
@@ -315,3 +319,144 @@ def rmp2(C, eps, eri, nocc):
     eo, ev = eps[:nocc], eps[nocc:]
     denom = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
     return float(np.sum(ovov * (2.0 * ovov - ovov.transpose(0, 3, 2, 1)) / denom))
+
+
+def half_overlap(S):
+    """S^{1/2} over the eigenvalues above the linear-dependence cut, as
+    Methods/hartree_fock.py:226-237 stores it (molecule.S)."""
+    s, U = np.linalg.eigh(S)
+    keep = s > LINEAR_DEPENDENCE
+    return (U[:, keep] * np.sqrt(s[keep])) @ U[:, keep].T
+
+
+def cuhf_constraint(S, Da, Db, Fa, Fb, na, nb):
+    """The CUHF constraint of Methods/hartree_fock.py:359-391 (constrain_UHF): natural
+    orbitals from eigh(S^1/2 (D_tot / 2) S^1/2) with coefficients (S^1/2)^-1 V, and the
+    core-virtual block of (F_a - F_b) / 2 in that basis cancelled: F_a + L, F_b - L."""
+    Sh = half_overlap(S)
+    P = Sh @ ((Da + Db) / 2.0) @ Sh
+    vals, vecs = np.linalg.eigh(P)
+    Cno = np.linalg.inv(Sh) @ vecs
+    back = np.linalg.inv(Cno)
+    idx = vals.argsort()[::-1]
+    nc, nact = nb, na - nb
+    core, virt = idx[:nc], idx[nc + nact:]
+    delta = Cno.T @ ((Fa - Fb) / 2.0) @ Cno
+    lam = np.zeros_like(delta)
+    lam[np.ix_(core, virt)] = -delta[np.ix_(core, virt)]
+    lam[np.ix_(virt, core)] = -delta[np.ix_(virt, core)]
+    lam = back.T @ lam @ back
+    return Fa + lam, Fb - lam
+
+
+class _SpinDIIS:
+    """Methods/hf_extensions/diis.py:14-154 for one spin: a residual enters the space
+    only while its largest element is below 0.5 (diis.py:22,32-34), C1 coefficients
+    (diis.py:108-112), the oldest vectors dropped while the B matrix's eigenvalue
+    condition number exceeds 1e7 (diis.py:87-96, Data/constants.py:36)."""
+
+    def __init__(self):
+        self.res, self.focks = [], []
+
+    def extrapolate(self, R, F):
+        if not abs(R.max()) < 0.5:
+            return F
+        self.res.append(R)
+        self.focks.append(F)
+        if len(self.res) < 2:
+            return F
+        while True:
+            m = len(self.res)
+            B = -np.ones((m + 1, m + 1))
+            B[m, m] = 0.0
+            for i in range(m):
+                for j in range(m):
+                    B[i, j] = np.trace(self.res[i] @ self.res[j].T)
+            ev = np.abs(np.linalg.eigvals(B))
+            cond = ev.max() / ev.min() if ev.min() > 0 else np.inf
+            if cond <= 1e7 or m == 1:
+                break
+            self.res.pop(0); self.focks.pop(0)
+        rhs = np.zeros(m + 1)
+        rhs[m] = -1.0
+        c = np.linalg.solve(B, rhs)[:m]
+        return sum(ci * Fi for ci, Fi in zip(c, self.focks))
+
+
+def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1e-9):
+    """Unrestricted (or constrained, cuhf=True) Hartree-Fock along the upstream path of
+    Methods/hartree_fock.py:23-142: core-Hamiltonian guess for both spins,
+    F_s = H + J[D_a + D_b] - K[D_s] (hartree_fock.py:329-355), the optional CUHF
+    constraint (hartree_fock.py:359-391), DIIS per spin (_SpinDIIS), aufbau occupation,
+    energy 0.5 sum(D_tot H + D_a F_a + D_b F_b) (hartree_fock.py:188-201) taken here
+    from the Fock matrices of the current densities; stops on |dE| < e_tol and a
+    density change below d_tol.  Returns dict(E, Ca, Cb, ea, eb, Da, Db, Fa, Fb,
+    iterations, converged)."""
+    X = orthogonaliser(S)
+    Xt = X.T
+
+    def diag(F):
+        e, Cp = np.linalg.eigh(Xt @ F @ X)
+        return e, X @ Cp
+
+    _, C = diag(H)
+    Da = C[:, :na] @ C[:, :na].T
+    Db = C[:, :nb] @ C[:, :nb].T
+
+    def focks(Da, Db):
+        J = np.einsum("cd,abcd->ab", Da + Db, eri, optimize=True)
+        Ka = np.einsum("cb,abcd->ad", Da, eri, optimize=True)
+        Kb = np.einsum("cb,abcd->ad", Db, eri, optimize=True)
+        Fa, Fb = H + J - Ka, H + J - Kb
+        if cuhf:
+            Fa, Fb = cuhf_constraint(S, Da, Db, Fa, Fb, na, nb)
+        return Fa, Fb
+
+    def energy(Da, Db, Fa, Fb):
+        return 0.5 * (np.sum((Da + Db) * H) + np.sum(Da * Fa) + np.sum(Db * Fb)) + e_nuc
+
+    da, db = _SpinDIIS(), _SpinDIIS()
+    E_old = None
+    drms = np.inf
+    converged = False
+    it = 0
+    for it in range(1, max_iter + 1):
+        Fa, Fb = focks(Da, Db)
+        E = energy(Da, Db, Fa, Fb)
+        if E_old is not None and abs(E - E_old) < e_tol and drms < d_tol:
+            converged = True
+            break
+        E_old = E
+        Fxa, Fxb = Fa, Fb
+        if it > 1:
+            Fxa = da.extrapolate(Xt @ (S @ Da @ Fa - Fa @ Da @ S) @ X, Fa)
+            Fxb = db.extrapolate(Xt @ (S @ Db @ Fb - Fb @ Db @ S) @ X, Fb)
+        ea, Ca = diag(Fxa)
+        eb, Cb = diag(Fxb)
+        Da_new = Ca[:, :na] @ Ca[:, :na].T
+        Db_new = Cb[:, :nb] @ Cb[:, :nb].T
+        drms = math.sqrt(np.mean((Da_new - Da) ** 2) + np.mean((Db_new - Db) ** 2))
+        Da, Db = Da_new, Db_new
+    ea, Ca = diag(Fa)
+    eb, Cb = diag(Fb)
+    return dict(E=E, Ca=Ca, Cb=Cb, ea=ea, eb=eb, Da=Da, Db=Db, Fa=Fa, Fb=Fb, iterations=it, converged=converged)
+
+
+def ump2(Ca, Cb, ea, eb, eri, na, nb):
+    """Unrestricted MP2 correlation energy, Methods/mp2.py:43-101: same-spin
+    sum over i >= j, p >= q of (<ip|jq> - <iq|jp>)^2 / D, opposite-spin sum of
+    <ip|jq>^2 / D, with the orbital energies of the final Fock matrices."""
+    def mo(C1, C2, o1, o2):
+        return np.einsum("pi,qa,rj,sb,pqrs->iajb", C1[:, :o1], C1[:, o1:], C2[:, :o2], C2[:, o2:], eri, optimize=True)
+
+    def same(C, e, o):
+        g = mo(C, C, o, o)
+        eo, ev = e[:o], e[o:]
+        den = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
+        t = g - g.transpose(0, 3, 2, 1)
+        return 0.25 * float(np.sum(t * t / den))
+
+    g = mo(Ca, Cb, na, nb)
+    den = (ea[:na, None, None, None] - ea[None, na:, None, None] + eb[None, None, :nb, None]
+           - eb[None, None, None, nb:])
+    return same(Ca, ea, na) + same(Cb, eb, nb) + float(np.sum(g * g / den))
