@@ -200,6 +200,13 @@ int pcg_expand_tasks(int nbra, const int *bra, const int *ket, const long long *
  * with density D (nbf x nbf); F = H + (G + G^T)/2 via pcg_fock_build. */
 int pcg_digest_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                      int ntask, const double *store, const double *D, double *G, void *stream);
+/* Unrestricted digestion (Methods/hartree_fock.py:329-355 with separate alpha and beta
+ * densities): GJ += the Coulomb part of (D_a + D_b)/2, GKa / GKb += the exchange parts
+ * of D_a / D_b, so that F_s = H + (G + G^T)/2 with G = GJ + GKs equals
+ * H + J[D_a + D_b] - K[D_s]. */
+int pcg_digest_class_u(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
+                       int ntask, const double *store, const double *Da, const double *Db, double *GJ,
+                       double *GKa, double *GKb, void *stream);
 int pcg_fock_build(int n, const double *H, const double *G, double *F, void *stream);
 /* Same for nblocks consecutive ld x ld blocks (an ensemble of molecules). */
 int pcg_fock_build_batched(int nblocks, int ld, const double *H, const double *G, double *F, void *stream);

@@ -122,6 +122,17 @@ int pcg_digest_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs
                            (cudaStream_t)stream);
 }
 
+int pcg_digest_class_u(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                       const double* store, const double* Da, const double* Db, double* GJ, double* GKa, double* GKb,
+                       void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs || !Da || !Db || !GJ || !GKa || !GKb) {
+    pcg_set_error("pcg_digest_class_u: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  return pcg_launch_digest_u(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, Da, Db, GJ, GKa,
+                             GKb, (cudaStream_t)stream);
+}
+
 int pcg_fock_build(int n, const double* H, const double* G, double* F, void* stream) {
   return pcg_launch_fock(n, H, G, F, (cudaStream_t)stream);
 }

@@ -204,13 +204,6 @@ int pcg_launch_eri(int cls, const DevBasis& b, const DevPairsExt& pr, const Boys
   return pcg_launch_eri_g5(cls, pr, bt, tasks, ntask, store, precision, s);
 }
 
-#define NS(l) (2 * (l) + 1)
-#define PCG_SHAPE_CASES(X)                                                                               \
-  X(0, 1, 1, 1, 1) X(1, 3, 1, 1, 1) X(2, 3, 1, 3, 1) X(3, 3, 3, 1, 1) X(4, 3, 3, 3, 1) X(5, 3, 3, 3, 3) \
-  X(6, 5, 1, 1, 1) X(7, 5, 1, 3, 1) X(8, 5, 1, 3, 3) X(9, 5, 1, 5, 1) X(10, 5, 3, 1, 1)                 \
-  X(11, 5, 3, 3, 1) X(12, 5, 3, 3, 3) X(13, 5, 3, 5, 1) X(14, 5, 3, 5, 3) X(15, 5, 5, 1, 1)             \
-  X(16, 5, 5, 3, 1) X(17, 5, 5, 3, 3) X(18, 5, 5, 5, 1) X(19, 5, 5, 5, 3) X(20, 5, 5, 5, 5)
-
 int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                       const double* store, const double* D, double* G, cudaStream_t s) {
   if (ntask <= 0) return PCG_OK;

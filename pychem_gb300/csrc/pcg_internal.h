@@ -38,5 +38,16 @@ int pcg_launch_pair_data_f32(int npp, const double* zeta, const double* PA, cons
 int pcg_launch_pair_ao(const DevBasis& b, int npair, const int* pA, const int* pB, int* ao4, cudaStream_t s);
 int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                       const double* store, const double* D, double* G, cudaStream_t s);
+int pcg_launch_digest_u(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
+                        const double* store, const double* Da, const double* Db, double* GJ, double* GKa,
+                        double* GKb, cudaStream_t s);
 int pcg_launch_dense(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                      const double* store, double* eri, cudaStream_t s);
+
+// Quartet block shapes (2la+1, 2lb+1, 2lc+1, 2ld+1) of the 21 ERI classes, for the
+// per-class kernel switches.
+#define PCG_SHAPE_CASES(X)                                                                               \
+  X(0, 1, 1, 1, 1) X(1, 3, 1, 1, 1) X(2, 3, 1, 3, 1) X(3, 3, 3, 1, 1) X(4, 3, 3, 3, 1) X(5, 3, 3, 3, 3) \
+  X(6, 5, 1, 1, 1) X(7, 5, 1, 3, 1) X(8, 5, 1, 3, 3) X(9, 5, 1, 5, 1) X(10, 5, 3, 1, 1)                 \
+  X(11, 5, 3, 3, 1) X(12, 5, 3, 3, 3) X(13, 5, 3, 5, 1) X(14, 5, 3, 5, 3) X(15, 5, 5, 1, 1)             \
+  X(16, 5, 5, 3, 1) X(17, 5, 5, 3, 3) X(18, 5, 5, 5, 1) X(19, 5, 5, 5, 3) X(20, 5, 5, 5, 5)

@@ -328,6 +328,19 @@ class GpuEngine:
         _lib.call("pcg_fock_build", n, _ptr(self.H), _ptr(G), _ptr(F), _stream())
         return F
 
+    def fock_u(self, Da, Db):
+        """Unrestricted Fock matrices F_s = H + J[D_a + D_b] - K[D_s] (nbf x nbf each)."""
+        n = self.nbf
+        G = torch.zeros(3, n, n, dtype=torch.float64, device=self.dev)
+        Da, Db = Da.contiguous(), Db.contiguous()
+        for cls, rec in self.classes.items():
+            for part, (tasks, ntask) in rec.items():
+                _lib.call("pcg_digest_class_u", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
+                          _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), _ptr(Da), _ptr(Db), _ptr(G[0]),
+                          _ptr(G[1]), _ptr(G[2]), _stream())
+        Ga, Gb = G[0] + G[1], G[0] + G[2]
+        return self.H + 0.5 * (Ga + Ga.T), self.H + 0.5 * (Gb + Gb.T)
+
     def dense_eri(self):
         """Dense nbf^4 tensor (8-fold symmetric fill), zero where screened out."""
         n = self.nbf

@@ -186,21 +186,26 @@ def ozaki_gemm(A, B, C, batch, M, N, K, sA, sB, sCb, nslice=6, accumulate=False)
     return C
 
 
-def mp2_transform(eri, Co, Cv, gemm="ozaki", nslice=6):
-    """(ia|jb) from the dense AO tensor by four quarter transforms.
-    gemm="fp64": cuBLAS DGEMM; gemm="ozaki": BF16 tensor cores with FP64 accuracy."""
+def mp2_transform(eri, Co, Cv, gemm="ozaki", nslice=6, Co2=None, Cv2=None):
+    """(ia|jb) from the dense AO tensor by four quarter transforms, i, a with Co, Cv
+    and j, b with Co2, Cv2 (default: the same; different for the opposite-spin block
+    of UMP2).  gemm="fp64": cuBLAS DGEMM; gemm="ozaki": BF16 tensor cores with FP64
+    accuracy."""
     n, o = Co.shape
     v = Cv.shape[1]
+    Co2 = Co if Co2 is None else Co2
+    Cv2 = Cv if Cv2 is None else Cv2
+    o2, v2 = Co2.shape[1], Cv2.shape[1]
     if gemm == "fp64":
         t1 = (Co.T @ eri.reshape(n, n ** 3)).reshape(o, n, n * n)        # (i nu | lam sig)
         t2 = torch.matmul(Cv.T, t1)                                       # (i a | lam sig)
         del t1
-        t3 = torch.matmul(Co.T, t2.reshape(o * v, n, n))                  # (i a | j sig)
+        t3 = torch.matmul(Co2.T, t2.reshape(o * v, n, n))                 # (i a | j sig)
         del t2
-        return torch.matmul(t3, Cv).reshape(o, v, o, v)                   # (i a | j b)
+        return torch.matmul(t3, Cv2).reshape(o, v, o2, v2)                # (i a | j b)
     dev = eri.device
     E = eri.reshape(-1)
-    Co, Cv = Co.contiguous(), Cv.contiguous()
+    Co, Cv, Co2, Cv2 = Co.contiguous(), Cv.contiguous(), Co2.contiguous(), Cv2.contiguous()
     # Y1[i][(b c d)] = sum_a Co[a][i] E[a][(b c d)]
     Y1 = torch.empty(o * n ** 3, dtype=torch.float64, device=dev)
     ozaki_gemm(Co, E, Y1, 1, o, n ** 3, n, (0, 1, o), (0, n ** 3, 1), 0, nslice)
@@ -208,14 +213,14 @@ def mp2_transform(eri, Co, Cv, gemm="ozaki", nslice=6):
     Y2 = torch.empty(o * v * n * n, dtype=torch.float64, device=dev)
     ozaki_gemm(Cv, Y1, Y2, o, v, n * n, n, (0, 1, v), (n ** 3, n * n, 1), v * n * n, nslice)
     del Y1
-    # Y3[(i a)][j][d] = sum_c Co[c][j] Y2[(i a)][c][d]
-    Y3 = torch.empty(o * v * o * n, dtype=torch.float64, device=dev)
-    ozaki_gemm(Co, Y2, Y3, o * v, o, n, n, (0, 1, o), (n * n, n, 1), o * n, nslice)
+    # Y3[(i a)][j][d] = sum_c Co2[c][j] Y2[(i a)][c][d]
+    Y3 = torch.empty(o * v * o2 * n, dtype=torch.float64, device=dev)
+    ozaki_gemm(Co2, Y2, Y3, o * v, o2, n, n, (0, 1, o2), (n * n, n, 1), o2 * n, nslice)
     del Y2
-    # T[(i a j)][b] = sum_d Y3[(i a j)][d] Cv[d][b]
-    T = torch.empty(o * v * o * v, dtype=torch.float64, device=dev)
-    ozaki_gemm(Y3, Cv, T, 1, o * v * o, v, n, (0, n, 1), (0, v, 1), 0, nslice)
-    return T.reshape(o, v, o, v)
+    # T[(i a j)][b] = sum_d Y3[(i a j)][d] Cv2[d][b]
+    T = torch.empty(o * v * o2 * v2, dtype=torch.float64, device=dev)
+    ozaki_gemm(Y3, Cv2, T, 1, o * v * o2, v2, n, (0, n, 1), (0, v2, 1), 0, nslice)
+    return T.reshape(o, v, o2, v2)
 
 
 def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6):
@@ -236,3 +241,160 @@ def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6):
 
 def mp2_flops(n, o, v):
     return 2.0 * o * n ** 4 + 2.0 * o * v * n ** 3 + 2.0 * o * o * v * n ** 2 + 2.0 * o * o * v * v * n
+
+
+# ------------------------------------------------------------------------------------
+# Open shells: UHF / CUHF and UMP2
+# ------------------------------------------------------------------------------------
+class _SpinDIIS:
+    """Per-spin Pulay DIIS as Methods/hf_extensions/diis.py:14-154: a residual enters
+    the space only while its largest element is below 0.5, C1 coefficients solved on
+    the host, the oldest vectors dropped while the B matrix's eigenvalue condition
+    number exceeds 1e7; the extrapolation runs on the GPU."""
+
+    def __init__(self):
+        self.res, self.focks = [], []
+        self.B = np.zeros((0, 0))
+
+    def extrapolate(self, R, F, row, rmax):
+        """R, F: this iteration's residual and Fock (device); row: inner products of R
+        with the stored residuals and itself (host); rmax: max element of R."""
+        if not abs(rmax) < 0.5:
+            return F, False
+        m = len(self.res) + 1
+        Bn = np.zeros((m, m))
+        Bn[:m - 1, :m - 1] = self.B
+        Bn[m - 1, :] = row
+        Bn[:, m - 1] = row
+        self.B = Bn
+        self.res.append(R)
+        self.focks.append(F)
+        if m < 2:
+            return F, True
+        while True:
+            m = len(self.res)
+            M = -np.ones((m + 1, m + 1))
+            M[:m, :m] = self.B
+            M[m, m] = 0.0
+            ev = np.abs(np.linalg.eigvals(M))
+            if (ev.min() > 0 and ev.max() / ev.min() <= 1e7) or m == 1:
+                break
+            self.res.pop(0); self.focks.pop(0)
+            self.B = self.B[1:, 1:]
+        rhs = np.zeros(m + 1)
+        rhs[m] = -1.0
+        c = np.linalg.solve(M, rhs)[:m]
+        cw = torch.tensor(c, dtype=torch.float64, device=F.device)
+        return torch.einsum("k,kij->ij", cw, torch.stack(self.focks)), True
+
+
+def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8):
+    """Unrestricted (cuhf=False) or constrained unrestricted Hartree-Fock on a prepared
+    GpuEngine, along Methods/hartree_fock.py:23-142: core-Hamiltonian guess for both
+    spins, Fock matrices from pcg_digest_class_u, the CUHF constraint of
+    hartree_fock.py:359-391 (natural orbitals of S^1/2 (D_tot/2) S^1/2, the core-virtual
+    block of (F_a - F_b)/2 cancelled), per-spin DIIS, aufbau occupation, energy
+    0.5 sum(D_tot H + D_a F_a + D_b F_b) (hartree_fock.py:188-201) from the Fock
+    matrices of the current densities.  Returns SCFResult with E, Ca, Cb, ea, eb, Da,
+    Db, iterations, converged."""
+    mol = engine.mol
+    na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+    S, H = engine.S, engine.H
+    dev = S.device
+    e_nuc = mol.nuclear_repulsion()
+    s, U = eigen.eigh(S)
+    if float(s.min()) <= LINEAR_DEPENDENCE:
+        raise ValueError("linear dependence in the basis; uhf needs a full-rank overlap")
+    X = U * s.rsqrt().unsqueeze(0)
+    Xt = X.T.contiguous()
+    Sh = (U * s.sqrt().unsqueeze(0)) @ U.T          # S^1/2 (hartree_fock.py:234-237)
+    Shi = X @ U.T                                   # (S^1/2)^-1
+
+    def diag(F):
+        e, Q = eigen.eigh(Xt @ F @ X)
+        return e, X @ Q
+
+    def constrain(Da, Db, Fa, Fb):
+        vals, V = eigen.eigh(Sh @ (0.5 * (Da + Db)) @ Sh)
+        Cno = Shi @ V
+        back = V.T @ Sh                             # Cno^-1
+        order = torch.argsort(vals, descending=True)
+        core, virt = order[:nb], order[na:]
+        delta = Cno.T @ (0.5 * (Fa - Fb)) @ Cno
+        lam = torch.zeros_like(delta)
+        lam[core.unsqueeze(1), virt.unsqueeze(0)] = -delta[core.unsqueeze(1), virt.unsqueeze(0)]
+        lam[virt.unsqueeze(1), core.unsqueeze(0)] = -delta[virt.unsqueeze(1), core.unsqueeze(0)]
+        lam = back.T @ lam @ back
+        return Fa + lam, Fb - lam
+
+    _, C = diag(H)
+    Da = C[:, :na] @ C[:, :na].T
+    Db = C[:, :nb] @ C[:, :nb].T
+    dia, dib = _SpinDIIS(), _SpinDIIS()
+    E_old = Da_old = Db_old = None
+    converged = False
+    it = 0
+    for it in range(1, max_iter + 1):
+        Fa, Fb = engine.fock_u(Da, Db)
+        if cuhf:
+            Fa, Fb = constrain(Da, Db, Fa, Fb)
+        Ra = Xt @ (S @ Da @ Fa - Fa @ Da @ S) @ X
+        Rb = Xt @ (S @ Db @ Fb - Fb @ Db @ S) @ X
+        vals = [0.5 * (torch.sum((Da + Db) * H) + torch.sum(Da * Fa) + torch.sum(Db * Fb)).reshape(1)]
+        if Da_old is not None:
+            vals.append(torch.sqrt(torch.mean((Da - Da_old) ** 2) + torch.mean((Db - Db_old) ** 2)).reshape(1))
+        else:
+            vals.append(torch.zeros(1, dtype=torch.float64, device=dev))
+        vals.append(torch.stack([Ra.max(), Rb.max()]))
+        ra, rb = Ra.reshape(-1), Rb.reshape(-1)
+        vals.append(torch.stack([torch.dot(ra, r.reshape(-1)) for r in dia.res] + [torch.dot(ra, ra)]))
+        vals.append(torch.stack([torch.dot(rb, r.reshape(-1)) for r in dib.res] + [torch.dot(rb, rb)]))
+        host = torch.cat(vals).cpu().numpy()
+        E = float(host[0]) + e_nuc
+        if E_old is not None and abs(E - E_old) < e_tol and float(host[1]) < d_tol:
+            converged = True
+            break
+        E_old, Da_old, Db_old = E, Da, Db
+        Fxa, Fxb = Fa, Fb
+        if it > 1:
+            k = len(dia.res) + 1
+            Fxa, _ = dia.extrapolate(Ra, Fa, host[4:4 + k], host[2])
+            Fxb, _ = dib.extrapolate(Rb, Fb, host[4 + k:], host[3])
+        _, Ca = diag(Fxa)
+        _, Cb = diag(Fxb)
+        Da = Ca[:, :na] @ Ca[:, :na].T
+        Db = Cb[:, :nb] @ Cb[:, :nb].T
+    ea, Ca = diag(Fa)
+    eb, Cb = diag(Fb)
+    return SCFResult(E=E, Ca=Ca, Cb=Cb, ea=ea, eb=eb, Da=Da, Db=Db, Fa=Fa, Fb=Fb, iterations=it,
+                     converged=converged)
+
+
+def ump2(engine, res, eri=None, gemm="ozaki", nslice=6):
+    """Unrestricted MP2 correlation energy (Methods/mp2.py:43-101): same-spin
+    0.25 sum ((ia|jb) - (ib|ja))^2 / D per spin and opposite-spin sum (ia|jb)^2 / D,
+    with the orbital energies of the final Fock matrices; the integrals from the four
+    quarter transforms of mp2_transform."""
+    mol = engine.mol
+    na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+    if eri is None:
+        eri = engine.dense_eri()
+    Ca, Cb, ea, eb = res.Ca, res.Cb, res.ea, res.eb
+
+    def same(C, e, o):
+        if o == 0 or o == C.shape[1]:
+            return 0.0
+        g = mp2_transform(eri, C[:, :o].contiguous(), C[:, o:].contiguous(), gemm=gemm, nslice=nslice)
+        eo, ev = e[:o], e[o:]
+        den = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
+        t = g - g.permute(0, 3, 2, 1)
+        return 0.25 * float(torch.sum(t * t / den))
+
+    e_ab = 0.0
+    if na and nb:
+        g = mp2_transform(eri, Ca[:, :na].contiguous(), Ca[:, na:].contiguous(), gemm=gemm, nslice=nslice,
+                          Co2=Cb[:, :nb].contiguous(), Cv2=Cb[:, nb:].contiguous())
+        den = (ea[:na, None, None, None] - ea[None, na:, None, None] + eb[None, None, :nb, None]
+               - eb[None, None, None, nb:])
+        e_ab = float(torch.sum(g * g / den))
+    return same(Ca, ea, na) + same(Cb, eb, nb) + e_ab
