@@ -383,15 +383,25 @@ class _SpinDIIS:
         return sum(ci * Fi for ci, Fi in zip(c, self.focks))
 
 
-def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1e-9):
+def mom_order(C_new, e_new, C_ref, n, S):
+    """Methods/hf_extensions/mom.py:6-47: order the new orbitals by decreasing
+    |sum_j <ref_j|new_i>| over the n occupied reference orbitals (stable sort)."""
+    p = np.abs((C_ref[:, :n].T @ S @ C_new).sum(axis=0))
+    order = np.argsort(-p, kind="stable")
+    return C_new[:, order], e_new[order]
+
+
+def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1e-9, C0=None, mom=False):
     """Unrestricted (or constrained, cuhf=True) Hartree-Fock along the upstream path of
     Methods/hartree_fock.py:23-142: core-Hamiltonian guess for both spins,
     F_s = H + J[D_a + D_b] - K[D_s] (hartree_fock.py:329-355), the optional CUHF
     constraint (hartree_fock.py:359-391), DIIS per spin (_SpinDIIS), aufbau occupation,
     energy 0.5 sum(D_tot H + D_a F_a + D_b F_b) (hartree_fock.py:188-201) taken here
     from the Fock matrices of the current densities; stops on |dE| < e_tol and a
-    density change below d_tol.  Returns dict(E, Ca, Cb, ea, eb, Da, Db, Fa, Fb,
-    iterations, converged)."""
+    density change below d_tol.  C0 = (Ca, Cb): starting orbitals (occupied columns
+    first) instead of the core guess; mom: occupy by maximum overlap with C0's
+    occupied orbitals (the FIXED reference of Methods/hf_extensions/mom.py) instead of
+    aufbau.  Returns dict(E, Ca, Cb, ea, eb, Da, Db, Fa, Fb, iterations, converged)."""
     X = orthogonaliser(S)
     Xt = X.T
 
@@ -399,9 +409,11 @@ def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1
         e, Cp = np.linalg.eigh(Xt @ F @ X)
         return e, X @ Cp
 
-    _, C = diag(H)
-    Da = C[:, :na] @ C[:, :na].T
-    Db = C[:, :nb] @ C[:, :nb].T
+    if C0 is None:
+        _, C = diag(H)
+        C0 = (C, C)
+    Da = C0[0][:, :na] @ C0[0][:, :na].T
+    Db = C0[1][:, :nb] @ C0[1][:, :nb].T
 
     def focks(Da, Db):
         J = np.einsum("cd,abcd->ab", Da + Db, eri, optimize=True)
@@ -433,12 +445,18 @@ def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1
             Fxb = db.extrapolate(Xt @ (S @ Db @ Fb - Fb @ Db @ S) @ X, Fb)
         ea, Ca = diag(Fxa)
         eb, Cb = diag(Fxb)
+        if mom:
+            Ca, ea = mom_order(Ca, ea, C0[0], na, S)
+            Cb, eb = mom_order(Cb, eb, C0[1], nb, S)
         Da_new = Ca[:, :na] @ Ca[:, :na].T
         Db_new = Cb[:, :nb] @ Cb[:, :nb].T
         drms = math.sqrt(np.mean((Da_new - Da) ** 2) + np.mean((Db_new - Db) ** 2))
         Da, Db = Da_new, Db_new
     ea, Ca = diag(Fa)
     eb, Cb = diag(Fb)
+    if mom:
+        Ca, ea = mom_order(Ca, ea, C0[0], na, S)
+        Cb, eb = mom_order(Cb, eb, C0[1], nb, S)
     return dict(E=E, Ca=Ca, Cb=Cb, ea=ea, eb=eb, Da=Da, Db=Db, Fa=Fa, Fb=Fb, iterations=it, converged=converged)
 
 

@@ -288,15 +288,26 @@ class _SpinDIIS:
         return torch.einsum("k,kij->ij", cw, torch.stack(self.focks)), True
 
 
-def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8):
+def mom_order(C, e, C_ref, n, S):
+    """Maximum overlap ordering (Methods/hf_extensions/mom.py:6-47): columns of C by
+    decreasing |sum_j <ref_j|C_i>| over the n occupied reference orbitals."""
+    p = ((C_ref[:, :n].T @ S) @ C).sum(dim=0).abs()
+    order = torch.argsort(-p, stable=True)
+    return C[:, order], e[order]
+
+
+def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=False):
     """Unrestricted (cuhf=False) or constrained unrestricted Hartree-Fock on a prepared
     GpuEngine, along Methods/hartree_fock.py:23-142: core-Hamiltonian guess for both
     spins, Fock matrices from pcg_digest_class_u, the CUHF constraint of
     hartree_fock.py:359-391 (natural orbitals of S^1/2 (D_tot/2) S^1/2, the core-virtual
     block of (F_a - F_b)/2 cancelled), per-spin DIIS, aufbau occupation, energy
     0.5 sum(D_tot H + D_a F_a + D_b F_b) (hartree_fock.py:188-201) from the Fock
-    matrices of the current densities.  Returns SCFResult with E, Ca, Cb, ea, eb, Da,
-    Db, iterations, converged."""
+    matrices of the current densities.  C0 = (Ca, Cb): starting orbitals, occupied
+    columns first (an excited determinant) instead of the core guess; mom: occupy by
+    maximum overlap with C0's occupied orbitals (the FIXED reference of
+    Methods/hf_extensions/mom.py) instead of aufbau.  Returns SCFResult with E, Ca, Cb,
+    ea, eb, Da, Db, iterations, converged."""
     mol = engine.mol
     na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
     S, H = engine.S, engine.H
@@ -327,9 +338,11 @@ def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8):
         lam = back.T @ lam @ back
         return Fa + lam, Fb - lam
 
-    _, C = diag(H)
-    Da = C[:, :na] @ C[:, :na].T
-    Db = C[:, :nb] @ C[:, :nb].T
+    if C0 is None:
+        _, C = diag(H)
+        C0 = (C, C)
+    Da = C0[0][:, :na] @ C0[0][:, :na].T
+    Db = C0[1][:, :nb] @ C0[1][:, :nb].T
     dia, dib = _SpinDIIS(), _SpinDIIS()
     E_old = Da_old = Db_old = None
     converged = False
@@ -360,12 +373,18 @@ def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8):
             k = len(dia.res) + 1
             Fxa, _ = dia.extrapolate(Ra, Fa, host[4:4 + k], host[2])
             Fxb, _ = dib.extrapolate(Rb, Fb, host[4 + k:], host[3])
-        _, Ca = diag(Fxa)
-        _, Cb = diag(Fxb)
+        ea, Ca = diag(Fxa)
+        eb, Cb = diag(Fxb)
+        if mom:
+            Ca, ea = mom_order(Ca, ea, C0[0], na, S)
+            Cb, eb = mom_order(Cb, eb, C0[1], nb, S)
         Da = Ca[:, :na] @ Ca[:, :na].T
         Db = Cb[:, :nb] @ Cb[:, :nb].T
     ea, Ca = diag(Fa)
     eb, Cb = diag(Fb)
+    if mom:
+        Ca, ea = mom_order(Ca, ea, C0[0], na, S)
+        Cb, eb = mom_order(Cb, eb, C0[1], nb, S)
     return SCFResult(E=E, Ca=Ca, Cb=Cb, ea=ea, eb=eb, Da=Da, Db=Db, Fa=Fa, Fb=Fb, iterations=it,
                      converged=converged)
 

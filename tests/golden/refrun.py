@@ -110,7 +110,10 @@ _EDITS = {
         ("(self.NElectrons + (self.Multiplicity-1))/2", "(self.NElectrons + (self.Multiplicity-1))//2"),
         ("(self.NElectrons - (self.Multiplicity-1))/2", "(self.NElectrons - (self.Multiplicity-1))//2"),
     ],
-    "Methods/hartree_fock.py": [("from itertools import izip", "izip = zip")],
+    "Methods/hartree_fock.py": [("from itertools import izip", "izip = zip"),
+                                # Python 2 compared an array with [] to a scalar True;
+                                # NumPy now compares elementwise
+                                ("elif this_state.Alpha.MOs != []:", "elif len(this_state.Alpha.MOs) != 0:")],
     "Methods/hf_extensions/diis.py": [("xrange", "range")],
     "Methods/basis_fit.py": [("xrange", "range")],
     "pychem.py": [("SafeConfigParser", "ConfigParser")],
@@ -184,7 +187,7 @@ def load(root):
 
 
 def molecule_from_spec(ns, coords, basis, charge=0, multiplicity=1, reference="RHF",
-                       units="ANGSTROM", method="HF", max_iter=200, outdir=None):
+                       units="ANGSTROM", method="HF", max_iter=200, outdir=None, extra=None):
     """Build reference Settings/Molecule objects from an in-memory INI section."""
     import configparser
     cp = configparser.ConfigParser()
@@ -200,6 +203,8 @@ def molecule_from_spec(ns, coords, basis, charge=0, multiplicity=1, reference="R
     cp.set(sec, "Coords", repr([[a[0], float(a[1]), float(a[2]), float(a[3]), float(a[4])] for a in coords]))
     cp.set(sec, "Reference", repr(reference))
     cp.set(sec, "Max_SCF_Iterations", repr(max_iter))
+    for key, value in (extra or {}).items():
+        cp.set(sec, key, repr(value))
     molecule, settings = ns["structures"].process_input(sec, cp)
     outdir = outdir or tempfile.mkdtemp(prefix="pychem_out_")
     settings.OutFile = open(os.path.join(outdir, "case.out"), "w")

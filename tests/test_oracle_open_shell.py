@@ -30,3 +30,16 @@ def test_example1_printed_output_agrees_loosely():
     |dE| < 1e-7 stop; the tight re-run of the same input is within 3e-6 of it."""
     ref = json.load(open(os.path.join(HERE, "golden", "open_shell_energies.json")))
     assert abs(ref["h3_cuhf_sto3g"]["E_scf"] - ref["example1_printed"]["printed_final_hf"]) < 3e-6
+
+
+@pytest.mark.parametrize("name", ["h2_mom_631g", "hf_mom_sto3g"])
+def test_mom_excited_states(name):
+    """Alpha HOMO -> LUMO excited states by the maximum overlap method, started from the
+    reference's reordered ground-state orbitals, as pychem.py runs them."""
+    g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    na, nb = int(g["n_alpha"]), int(g["n_beta"])
+    r0 = O.uhf(g["S"], g["H"], g["eri_dense"], na, nb, float(g["E_nuc"]))
+    assert abs(r0["E"] - float(g["E_ground"])) < 1e-9
+    r1 = O.uhf(g["S"], g["H"], g["eri_dense"], na, nb, float(g["E_nuc"]), C0=(g["start_alpha"], g["start_beta"]),
+               mom=True)
+    assert r1["converged"] and abs(r1["E"] - float(g["E_excited"])) < 1e-9
