@@ -150,7 +150,8 @@ class GpuEngine:
         self.nbf = self.mol.NOrbitals
 
     def _build_pairs(self):
-        """All shell pairs a <= b, oriented so that l_A >= l_B; kinds = (l_A, l_B, nA, nB)."""
+        """All shell pairs a <= b, oriented so that l_A >= l_B (their kinds are set by
+        compute_pair_data)."""
         a = self.h_basis
         ns = len(a["sh_l"])
         ia, ib = np.triu_indices(ns)
@@ -169,43 +170,73 @@ class GpuEngine:
         self.npair = len(A)
         tot = int(npp.sum())
         dv = self.dev
-        self.pd = dict(A=self._t(A), B=self._t(B), ppoff=self._t(ppoff), npp=self._t(npp),
-                       AB=torch.empty(self.npair * 3, dtype=torch.float64, device=dv),
-                       zeta=torch.empty(tot, dtype=torch.float64, device=dv),
-                       P=torch.empty(tot * 3, dtype=torch.float64, device=dv),
-                       PA=torch.empty(tot * 3, dtype=torch.float64, device=dv),
-                       K=torch.empty(tot, dtype=torch.float64, device=dv),
-                       Kf=torch.empty(tot, dtype=torch.float32, device=dv),
-                       oo2z=torch.empty(tot, dtype=torch.float64, device=dv),
-                       ao4=torch.empty(self.npair * 4, dtype=torch.int32, device=dv),
-                       pf8=torch.empty(tot * 8, dtype=torch.float32, device=dv))
-        p = self.pd
-        t = PairsT()
-        t.npair = self.npair; t.npp = tot
+        # every primitive pair (pcg_pair_data writes these) ...
+        self.pd_full = dict(ppoff=self._t(ppoff), npp=self._t(npp),
+                            zeta=torch.empty(tot, dtype=torch.float64, device=dv),
+                            P=torch.empty(tot * 3, dtype=torch.float64, device=dv),
+                            PA=torch.empty(tot * 3, dtype=torch.float64, device=dv),
+                            K=torch.empty(tot, dtype=torch.float64, device=dv),
+                            Kf=torch.empty(tot, dtype=torch.float32, device=dv),
+                            oo2z=torch.empty(tot, dtype=torch.float64, device=dv))
+        # ... and the kept ones, which the ERI kernels read (filled by compute_pair_data)
+        self.pd = dict(A=self._t(A), B=self._t(B), AB=torch.empty(self.npair * 3, dtype=torch.float64, device=dv),
+                       ao4=torch.empty(self.npair * 4, dtype=torch.int32, device=dv))
+        self.pairs_t = PairsT()
+        self.compute_pair_data()
+
+    # primitive pairs with |K_p| max|K| below this are dropped (0 keeps all): every
+    # primitive-quartet term of an integral carries the factor K_P K_Q
+    prim_tau = 1e-20
+
+    def _set_pairs_t(self):
+        p, t = self.pd, self.pairs_t
+        t.npair = self.npair
+        t.npp = int(p["zeta"].numel())
         for k, f in (("A", "A"), ("B", "B"), ("ppoff", "ppoff"), ("npp", "npp_of"), ("AB", "AB"), ("zeta", "zeta"),
                      ("P", "P"), ("PA", "PA"), ("K", "K"), ("oo2z", "oo2z"), ("Kf", "Kf"), ("ao4", "ao4"), ("pf8", "pf8")):
             setattr(t, f, p[k].data_ptr())
-        self.pairs_t = t
-        # pair kinds ordered by (pair class, nA, nB)
+
+    def _compact_primitives(self):
+        """Keep the primitive pairs with |K_p| max|K| >= prim_tau, pair by pair (each
+        pair's kept primitives stay contiguous), and re-derive the pair kinds
+        (pair class, kept primitive pairs) that bucket the quartets."""
+        f, p = self.pd_full, self.pd
+        keep = f["K"].abs() * f["K"].abs().max() >= self.prim_tau
+        idx = keep.nonzero().squeeze(1)
+        cs = torch.cat([torch.zeros(1, dtype=torch.int64, device=self.dev), torch.cumsum(keep.to(torch.int64), 0)])
+        start = f["ppoff"].to(torch.int64)
+        cnt = cs[start + f["npp"].to(torch.int64)] - cs[start]
+        p["ppoff"] = cs[start].to(torch.int32)
+        p["npp"] = cnt.to(torch.int32)
+        p["zeta"] = f["zeta"][idx]
+        p["K"] = f["K"][idx]
+        p["Kf"] = f["Kf"][idx]
+        p["oo2z"] = f["oo2z"][idx]
+        p["P"] = f["P"].view(-1, 3)[idx].reshape(-1)
+        p["PA"] = f["PA"].view(-1, 3)[idx].reshape(-1)
+        p["pf8"] = torch.empty(idx.numel() * 8, dtype=torch.float32, device=self.dev)
+        # pair kinds ordered by (pair class, kept primitive pairs)
+        npp = cnt.cpu().numpy().astype(np.int64)
         pc = pair_class(self.h_pairs["lA"], self.h_pairs["lB"]).astype(np.int64)
-        ma, mb = int(nA.max()) + 1, int(nB.max()) + 1
-        code = (pc * ma + nA) * mb + nB          # increasing in (pair class, nA, nB)
-        uniq, inv = np.unique(code, return_inverse=True)
-        self.kinds = [(int(c // (ma * mb)), int(c // mb % ma), int(c % mb)) for c in uniq]
+        mb = int(npp.max()) + 1
+        uniq, inv = np.unique(pc * mb + npp, return_inverse=True)
+        self.kinds = [(int(c // mb), int(c % mb)) for c in uniq]
         self.pair_kind = np.asarray(inv).ravel().astype(np.int32)
-        self.compute_pair_data()
 
     def compute_pair_data(self):
-        """Primitive-pair data, the per-pair AO table and the packed FP32 primitive-pair
-        table from the device-resident shells (three kernels)."""
-        p = self.pd
-        _lib.call("pcg_pair_data", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ppoff"]),
-                  _ptr(p["AB"]), _ptr(p["zeta"]), _ptr(p["P"]), _ptr(p["PA"]), _ptr(p["K"]), _ptr(p["Kf"]),
-                  _ptr(p["oo2z"]), _stream())
+        """Primitive-pair data of every pair, the negligible primitive pairs dropped
+        (_compact_primitives), the per-pair AO table and the packed FP32 primitive-pair
+        table, from the device-resident shells."""
+        p, f = self.pd, self.pd_full
+        _lib.call("pcg_pair_data", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(f["ppoff"]),
+                  _ptr(p["AB"]), _ptr(f["zeta"]), _ptr(f["P"]), _ptr(f["PA"]), _ptr(f["K"]), _ptr(f["Kf"]),
+                  _ptr(f["oo2z"]), _stream())
+        self._compact_primitives()
         _lib.call("pcg_pair_ao", ctypes.byref(self.basis_t), self.npair, _ptr(p["A"]), _ptr(p["B"]), _ptr(p["ao4"]),
                   _stream())
         _lib.call("pcg_pair_data_f32", int(p["zeta"].numel()), _ptr(p["zeta"]), _ptr(p["PA"]), _ptr(p["oo2z"]),
                   _ptr(p["Kf"]), _ptr(p["pf8"]), _stream())
+        self._set_pairs_t()
 
     # ---------------------------------------------------------------------------------
     def one_electron(self):
@@ -258,7 +289,7 @@ class GpuEngine:
             for j in range(i + 1):
                 ct[i, j] = lib.pcg_eri_class_id(int(kl[i, 0]), int(kl[i, 1]), int(kl[j, 0]), int(kl[j, 1]))
         mol, nmol = self._pair_molecule()
-        work = torch.as_tensor([k[1] * k[2] for k in self.kinds], dtype=torch.int64, device=dev)
+        work = torch.as_tensor([k[1] for k in self.kinds], dtype=torch.int64, device=dev)
         plan, ket_list = plan_quartets(self.Q, torch.as_tensor(self.pair_kind, dtype=torch.int64, device=dev), mol,
                                        nmol, torch.as_tensor(ct, device=dev), float(self.threshold),
                                        float(self.fp32_below), kind_work=work)
