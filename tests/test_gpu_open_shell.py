@@ -72,3 +72,28 @@ def test_mom_excited_states_against_reference(name):
     # here; the energy is stationary there (its error is quadratic in the density's)
     r1 = uhf(eng, C0=C0, mom=True, d_tol=1e-6)
     assert r1.converged and abs(r1.E - float(g["E_excited"])) < 1e-8
+
+
+def test_command_line_runner(tmp_path):
+    """An input file in the reference's format (the H3 doublet of the CUHF + MP2
+    fixture and the H2 HOMO -> LUMO MOM fixture, coordinates in bohr) through
+    python -m pychem_gb300's runner."""
+    from pychem_gb300.cli import run_file
+    g1 = np.load(os.path.join(HERE, "golden", "h3_cuhf_sto3g.npz"))
+    g2 = np.load(os.path.join(HERE, "golden", "h2_mom_631g.npz"))
+
+    def coords(g):
+        return repr([[str(a), float(z), *map(float, xyz)] for a, z, xyz in zip(g["atoms"], g["charges"],
+                                                                               g["coords_bohr"])])
+    p = tmp_path / "jobs.inp"
+    p.write_text('[h3]\nMethod = "MP2"\nBasis_Sets = ["STO-3G"]\nMultiplicity = 2\nCharge = 0\n'
+                 'Coords_Units = "BOHR"\nCoords = %s\nReference = "CUHF"\n'
+                 '[h2]\nMethod = "HF"\nBasis_Sets = ["6-31G"]\nCoords_Units = "BOHR"\nCoords = %s\n'
+                 'Reference = "UHF"\nExcitations = "HOMO-LUMO"\n' % (coords(g1), coords(g2)))
+    res = run_file(str(p), stream=open(os.devnull, "w"))
+    h3, h2 = res[0]["states"][0], res[1]["states"]
+    assert abs(h3["E_hf"] - float(g1["E_scf"])) < 1e-8
+    assert abs(h3["E_mp2_corr"] - float(g1["E_mp2_corr"])) < 1e-8
+    assert abs(h2[0]["E_hf"] - float(g2["E_ground"])) < 1e-8
+    assert abs(h2[1]["E_hf"] - float(g2["E_excited"])) < 1e-8
+    assert (tmp_path / "h3.out").exists() and (tmp_path / "h2.out").exists()
