@@ -27,7 +27,26 @@ from . import eigen
 LINEAR_DEPENDENCE = 1.0e-6   # Data/constants.py:34
 
 
-def orthogonaliser(S):
+def orthogonaliser(S, canonical=False):
+    """X with X^T S X = I.  Upstream (hartree_fock.py:226-237) uses the canonical
+    U s^-1/2 with eigenvalues s <= 1e-6 dropped.  Unless canonical=True, a Cholesky
+    factor is used instead, X = L^-T, when the smallest eigenvalue of S (estimated by
+    power iteration on S^-1 = L^-T L^-1) is above 1e-5: then nothing would be dropped
+    and energies and orbitals do not depend on the choice of X; otherwise the canonical
+    route."""
+    if not canonical and S.shape[0] > eigen.FP64_JACOBI_MAX_N:
+        L, info = torch.linalg.cholesky_ex(S)
+        if int(info) == 0:
+            n = S.shape[0]
+            Li = torch.linalg.solve_triangular(L, torch.eye(n, dtype=S.dtype, device=S.device), upper=False)
+            v = torch.ones(n, dtype=S.dtype, device=S.device) / math.sqrt(n)
+            mu = torch.zeros((), dtype=S.dtype, device=S.device)
+            for _ in range(12):
+                w = Li.T @ (Li @ v)
+                mu = torch.linalg.vector_norm(w)
+                v = w / mu
+            if 1.0 / float(mu) > 10.0 * LINEAR_DEPENDENCE:
+                return Li.T.contiguous()
     s, U = eigen.eigh(S, exact=True)
     s = torch.flip(s, [0])
     U = torch.flip(U, [1])
@@ -166,7 +185,8 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
         Qo = state["Q"][:, :nocc]
         Dp = Qo @ Qo.T
     # orbitals of the final Fock matrix, exact (including inside near-degenerate
-    # clusters) for MP2's denominators
+    # clusters) for MP2's denominators; the refined vectors of the last iterations are
+    # converged only as an occupied/virtual split
     eps, C = diagonalise(Xt @ F @ X, exact=True)
     return SCFResult(E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=C, eps=eps, D=D, F=F, iterations=it,
                      converged=converged, history=history, fock_builds=it)
