@@ -1,10 +1,12 @@
-"""Closed-shell SCF and MP2 on the GPU.
+"""SCF and MP2 on the GPU: RHF (rhf), UHF / CUHF with MOM (uhf), RMP2 (rmp2), UMP2
+(ump2).
 
 Mirrors the upstream flow (``Methods/hartree_fock.py:23-154``): nuclear repulsion,
-core and overlap matrices, canonical orthogonalisation X = U s^{-1/2} with
-eigenvalues sorted descending and s <= 1e-6 dropped (``hartree_fock.py:226-237``),
-core guess (``hartree_fock.py:55-57``), then iterations of Fock build, Pulay DIIS on
-the residual X^T(SDF - FDS)X (``Methods/hf_extensions/diis.py:48-139``),
+core and overlap matrices, an orthogonaliser X (upstream's canonical U s^{-1/2} with
+s <= 1e-6 dropped, ``hartree_fock.py:226-237``, or a Cholesky factor when no
+eigenvalue is near that cut), a starting density (SAD by default; upstream's core
+guess, ``hartree_fock.py:55-57``, on request), then iterations of Fock build, Pulay
+DIIS on the residual X^T(SDF - FDS)X (``Methods/hf_extensions/diis.py:48-139``),
 diagonalisation of X^T F X and the occupied-orbital density
 (``hartree_fock.py:168-184``).
 
@@ -14,7 +16,8 @@ DIIS-extrapolated matrix, ``hartree_fock.py:105-108,131-133``, which is
 non-variational and lets its loop report energies of diverged runs), and convergence
 needs both |dE| < ``e_tol`` and RMS(dD) < ``d_tol`` (upstream: |dE| < 1e-7 only).
 
-MP2 is the closed-shell form of ``Methods/mp2.py:43-94`` (identical value for RHF).
+RMP2 is the closed-shell form of ``Methods/mp2.py:43-94`` (identical value for RHF);
+the AO->MO transforms run on BF16 tensor cores with FP64 accuracy (ozaki_gemm).
 """
 import math
 import time
