@@ -478,3 +478,140 @@ def ump2(Ca, Cb, ea, eb, eri, na, nb):
     den = (ea[:na, None, None, None] - ea[None, na:, None, None] + eb[None, None, :nb, None]
            - eb[None, None, None, nb:])
     return same(Ca, ea, na) + same(Cb, eb, nb) + float(np.sum(g * g / den))
+
+
+# ------------------------------------------------------------------------------------
+# NOCI (Methods/noci.py)
+# ------------------------------------------------------------------------------------
+NOCI_THRESH = 1.0e-8                # Data/constants.py:37
+
+
+def noci_biorthogonalize(C1, C2, S, n):
+    """Methods/noci.py:183-205: Lowdin-paired occupied orbitals from the SVD of
+    C1_o^T S C2_o; a pair whose plain (unit-metric) dot product is negative has the
+    second orbital's sign flipped."""
+    A, B = C1[:, :n], C2[:, :n]
+    U, _, Vt = np.linalg.svd(A.T @ S @ B)
+    A2, B2 = A @ U, B @ Vt.T
+    flip = np.einsum("pi,pi->i", A2, B2) < 0
+    B2[:, flip] *= -1.0
+    return A2, B2
+
+
+def noci_coulomb_exchange(Wa, Wb, eri):
+    """Methods/hartree_fock.py:345-347 on co-densities: J[W_a + W_b] and the exchange
+    matrices -K[W_s] with K_ad = sum_bc (ab|cd) W_cb."""
+    J = np.einsum("cd,abcd->ab", Wa + Wb, eri, optimize=True)
+    Xa = np.einsum("cb,abcd->ad", -Wa, eri, optimize=True)
+    Xb = np.einsum("cb,abcd->ad", -Wb, eri, optimize=True)
+    return J, Xa, Xb
+
+
+def noci_element(Ca1, Cb1, Ca2, Cb2, S, H, eri, na, nb, e_nuc):
+    """One CI matrix element and overlap, Methods/noci.py:63-106: Lowdin pairing of
+    each spin, then noci_element_paired."""
+    a1, a2 = noci_biorthogonalize(Ca1, Ca2, S, na)
+    b1, b2 = noci_biorthogonalize(Cb1, Cb2, S, nb)
+    return noci_element_paired(a1, a2, b1, b2, S, H, eri, na, nb, e_nuc)
+
+
+def noci_zero_counts(a1, a2, b1, b2, S):
+    """Numbers of paired overlaps at or below NOCI_THRESH in each spin."""
+    ov_a = np.diagonal(a1.T @ S @ a2)
+    ov_b = np.diagonal(b1.T @ S @ b2)
+    return int((ov_a <= NOCI_THRESH).sum()), int((ov_b <= NOCI_THRESH).sum())
+
+
+def noci_element_paired(a1, a2, b1, b2, S, H, eri, na, nb, e_nuc):
+    """The element from given paired orbitals, Methods/noci.py:65-106 with the helpers
+    of noci.py:207-318: reduced overlap over the paired overlaps above NOCI_THRESH,
+    the no-zero, one-zero and two-zero forms (the two-zero form uses the first zero's
+    index in both spins, as upstream), 0 for more zeros; then times the reduced
+    overlap plus E_nuc times the determinant overlap.  With two zeros in one spin the
+    zero singular value is degenerate and the upstream form depends on the basis the
+    SVD picks inside that null space; given the same pairing it is exact."""
+    a1, a2, b1, b2 = a1.copy(), a2.copy(), b1.copy(), b2.copy()
+    core_a = a1.T @ H @ a2
+    core_b = b1.T @ H @ b2
+    ov_a = np.diagonal(a1.T @ S @ a2).copy()
+    ov_b = np.diagonal(b1.T @ S @ b2).copy()
+    s_state = float(np.prod(ov_a) * np.prod(ov_b))
+    reduced = 1.0
+    zeros = []
+    for spin, ov in (("a", ov_a), ("b", ov_b)):
+        for i, o in enumerate(ov):
+            if o > NOCI_THRESH:
+                reduced *= o
+            else:
+                zeros.append((i, spin))
+    if na > nb:                      # noci.py:81-84: beta padded to the alpha width
+        ov_b = np.concatenate([ov_b, np.ones(na - nb)])
+        b1 = np.concatenate([b1, np.zeros((b1.shape[0], na - nb))], axis=1)
+        b2 = np.concatenate([b2, np.zeros((b2.shape[0], na - nb))], axis=1)
+
+    def weighted(x1, x2, ov):
+        keep = ov > NOCI_THRESH
+        return (x1[:, keep] / ov[keep]) @ x2[:, keep].T
+
+    def inner(m1, m2):
+        return float(np.sum(m1 * m2))
+
+    if len(zeros) == 0:
+        Wa, Wb = weighted(a1, a2, ov_a), weighted(b1, b2, ov_b)
+        J, Xa, Xb = noci_coulomb_exchange(Wa, Wb, eri)
+        elem = 0.5 * (inner(Wa + Wb, J) + inner(Wa, Xa) + inner(Wb, Xb))
+        elem += sum(core_a[i, i] / ov_a[i] for i in range(na) if ov_a[i] > NOCI_THRESH)
+        elem += sum(core_b[i, i] / ov_b[i] for i in range(nb) if ov_b[i] > NOCI_THRESH)
+    elif len(zeros) == 1:
+        z, spin = zeros[0]
+        Wa, Wb = weighted(a1, a2, ov_a), weighted(b1, b2, ov_b)
+        J, Xa, Xb = noci_coulomb_exchange(Wa, Wb, eri)
+        x1, x2, X, core = (a1, a2, Xa, core_a) if spin == "a" else (b1, b2, Xb, core_b)
+        P = np.outer(x1[:, z], x2[:, z])
+        elem = inner(P, J) + inner(P, X) + core[z, z]
+    elif len(zeros) == 2:
+        z, spin = zeros[0]
+        Pa, Pb = np.outer(a1[:, z], a2[:, z]), np.outer(b1[:, z], b2[:, z])
+        J, Xa, Xb = noci_coulomb_exchange(Pa, Pb, eri)
+        P, X = (Pa, Xa) if spin == "a" else (Pb, Xb)
+        elem = inner(P, J) + inner(P, X)
+    else:
+        elem = 0.0
+    return elem * reduced + e_nuc * s_state, s_state
+
+
+def noci(dets_a, dets_b, S, H, eri, na, nb, e_nuc):
+    """Methods/noci.py:51-109: the CI matrix and overlap over the determinants (lower
+    triangle computed with state i as the bra, mirrored), then the generalised
+    symmetric eigenproblem (scipy.linalg.eigh).  Returns (energies, vectors, Hci, Sci)."""
+    from scipy.linalg import eigh
+    m = len(dets_a)
+    Hci = np.zeros((m, m))
+    Sci = np.zeros((m, m))
+    for i in range(m):
+        for j in range(i + 1):
+            h, s = noci_element(dets_a[i], dets_b[i], dets_a[j], dets_b[j], S, H, eri, na, nb, e_nuc)
+            Hci[i, j] = Hci[j, i] = h
+            Sci[i, j] = Sci[j, i] = s
+    e, v = eigh(Hci, Sci)
+    return e, v, Hci, Sci
+
+
+def noci_assemble(occupancy, C, hf_occupancy):
+    """Methods/noci.py:127-146: orbitals of a spin-flip determinant from a Hartree-Fock
+    state's orbitals: occupied columns (each must be occupied in that state) first in
+    order, the unoccupied ones after them."""
+    occupancy = list(occupancy)
+    out = np.zeros_like(C)
+    n_occ = sum(occupancy)
+    k_occ, k_virt = 0, n_occ
+    for i, o in enumerate(occupancy):
+        if o == 0:
+            out[:, k_virt] = C[:, i]
+            k_virt += 1
+        elif o == 1 and hf_occupancy[i] == 1:
+            out[:, k_occ] = C[:, i]
+            k_occ += 1
+        else:
+            raise ValueError("spin-flip determinant needs an orbital its Hartree-Fock state leaves empty")
+    return out

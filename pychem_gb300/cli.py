@@ -11,7 +11,9 @@ calculation runs in the last one; the upstream basis-fitting bootstrap through t
 earlier ones only supplies starting orbitals), ``Coords``, ``Coords_Units`` (ANGSTROM,
 BOHR), ``Charge``, ``Multiplicity``, ``Max_SCF_Iterations``, ``Excitations`` (HOMO-LUMO:
 the alpha HOMO -> LUMO state by MOM after the ground state, as ``pychem.py:64-86``),
-``Job_Type`` / ``Property_Type``.  Scattering properties and NOCI are not part of this
+``Constrain_Excited``, ``Job_Type`` / ``Property_Type``.  ``Method = "NOCI"`` runs the
+states of any ``Excitations`` keyword (spin-flip lists included) and the NOCI of
+``Methods/noci.py`` (pychem_gb300.noci).  Scattering properties are not part of this
 build: such sections run their Hartree-Fock part and report the rest as unavailable.
 """
 import ast
@@ -21,6 +23,7 @@ import sys
 
 import torch
 
+from . import noci
 from .engine import GpuEngine
 from .molecule import Molecule
 from .scf import rhf, rmp2, uhf, ump2
@@ -60,6 +63,23 @@ def run_section(name, opts, write):
     eng = GpuEngine(mol).prepare()
     res = {"section": name, "basis": basis, "reference": ref, "nbf": mol.NOrbitals}
     write("Section %s: %s/%s %s, %d basis functions" % (name, ref, basis, method, mol.NOrbitals))
+    if method.startswith("NOCI"):
+        out = noci.run(eng, opts.get("EXCITATIONS"), reference=ref,
+                       constrain_excited=bool(opts.get("CONSTRAIN_EXCITED", ref == "CUHF")),
+                       max_iter=max(max_iter, 300))
+        res["states"] = []
+        for k, st in enumerate(out["hf"]):
+            write("State %d: Final HF energy: %.11f (%d iterations%s)" % (k, st.E, st.iterations,
+                                                                       "" if st.converged else ", not converged"))
+            res["states"].append({"label": str(k), "E_hf": st.E, "iterations": st.iterations,
+                                  "converged": bool(st.converged)})
+        e = out["energies"].cpu().tolist()
+        res["noci_energies"] = e
+        write("NOCI determinants: %d" % len(out["dets_alpha"]))
+        write("NOCI energies: " + " ".join("%.11f" % x for x in e))
+        if opts.get("JOB_TYPE") == "PROPERTY":
+            write("Property %s: not available in this build" % opts.get("PROPERTY_TYPE"))
+        return res
     if ref == "RHF":
         if mol.NAlphaElectrons != mol.NBetaElectrons:
             raise ValueError("section %s: RHF needs a closed-shell molecule" % name)
@@ -86,8 +106,6 @@ def run_section(name, opts, write):
             entry["E_mp2_corr"] = e2
             write("State %s: MP2 correlation energy: %.11f  Total MP2 energy: %.11f" % (label, e2, st.E + e2))
         res["states"].append(entry)
-    if method.startswith("NOCI"):
-        write("NOCI: not available in this build")
     if opts.get("JOB_TYPE") == "PROPERTY":
         write("Property %s: not available in this build" % opts.get("PROPERTY_TYPE"))
     return res

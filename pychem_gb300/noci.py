@@ -1,0 +1,456 @@
+"""Non-orthogonal configuration interaction over Hartree-Fock determinants, on the GPU.
+
+The reference's NOCI (``Methods/noci.py``) runs after the Hartree-Fock states that
+``Util/structures.py:526-620`` (set_excitations) lists.  This module builds those states
+(excited_states), runs their SCFs in the reference's order with its starting orbitals
+(hf_states, ``pychem.py:62-93``), rearranges orbitals into spin-flip determinants
+(determinants, ``noci.py:127-173``) and evaluates the CI matrix (noci_matrix,
+``noci.py:51-109``):
+
+* Lowdin pairing of each pair's occupied orbitals by a batched SVD of C1_o^T S C2_o, the
+  second orbital of a pair sign-flipped when its plain dot product with the first is
+  negative (``noci.py:183-205``);
+* paired overlaps, the reduced overlap over those above 1e-8 and the zero list
+  (``noci.py:215-223``); co-densities W = sum_i c1_i c2_i^T / s_i, or the pair densities
+  P of a zero (``noci.py:207-213,261-300``);
+* J[W] and K[W] of every co-density from the ERI store by the unrestricted digestion
+  kernel (GpuEngine.coulomb_exchange), the matrix elements of the no-, one- and
+  two-zero forms (``noci.py:243-300``; the two-zero form takes the first zero's index in
+  both spins, as upstream), 0 for more zeros, times the reduced overlap plus E_nuc
+  times the determinant overlap;
+* the generalised eigenproblem H v = E S v by a Cholesky factor of S and the FP64
+  eigensolver (``noci.py:109``, scipy.linalg.eigh upstream).
+"""
+import torch
+
+from . import eigen
+from .molecule import N_ELECTRONS
+from .scf import uhf
+
+NOCI_THRESH = 1.0e-8          # Data/constants.py:37
+
+CORE_ORBITALS = ((2, 0), (10, 1), (18, 5), (36, 9))   # Data/constants.py:10-13 by nuclear charge
+
+
+def n_core_orbitals(charges):
+    """Frozen-core orbital count of a molecule (Data/constants.py:10-13)."""
+    total = 0
+    for z in charges:
+        for zmax, nc in CORE_ORBITALS:
+            if z <= zmax:
+                total += nc
+                break
+        else:
+            raise ValueError("no core-orbital count for Z = %d" % z)
+    return total
+
+
+# ------------------------------------------------------------------------------------
+# State lists (Util/structures.py:526-763)
+# ------------------------------------------------------------------------------------
+def _singles(o0, o1, v0, v1):
+    return [[i, a] for i in range(o0, o1) for a in range(v0, v1)]
+
+
+def _doubles(o0, o1, v0, v1):
+    return [[i, j, a, b] for i in range(o0, o1) for j in range(i + 1, o1)
+            for a in range(v0, v1) for b in range(a + 1, v1)]
+
+
+def _excite(ground, ex):
+    occ = list(ground)
+    occ[ex[0]], occ[ex[1]] = 0, 1
+    return occ
+
+
+def _excite2(ground, ex):
+    occ = list(ground)
+    occ[ex[0]] = occ[ex[1]] = 0
+    occ[ex[2]] = occ[ex[3]] = 1
+    return occ
+
+
+def _spinflip_states(alpha, beta, na, nb, level, istate):
+    """Util/structures.py:721-746.  Mutates ``beta`` and stores the two lists
+    themselves in its first entry, as upstream does: a later call that changes them
+    changes that entry too."""
+    beta[nb - 1] = 0
+    beta[na] = 1
+    out = []
+    if level == 1:
+        out.append([level, alpha, beta])
+        for i in range(nb - 1, na):
+            a, b = list(alpha), list(beta)
+            a[i], b[i] = 0, 1
+            a[na], b[na] = 1, 0
+            out.append([istate, a, b])
+    if level == 2:
+        beta[nb - 2] = 0
+        beta[na + 1] = 1
+        out.append([level, alpha, beta])
+        for i in range(nb - 2, na):
+            for k in range(na, na + 2):
+                a, b = list(alpha), list(beta)
+                a[i], b[i] = 0, 1
+                a[k], b[k] = 1, 0
+                out.append([level, a, b])
+            for j in range(i, na):
+                a, b = list(alpha), list(beta)
+                a[i] = a[j] = 0
+                b[i] = b[j] = 1
+                a[na] = a[na + 1] = 1
+                b[na] = b[na + 1] = 0
+                out.append([istate, a, b])
+    return out
+
+
+def _ci_states(alpha, beta, na, nb, ci_level, sf_level, istate):
+    """Util/structures.py:750-798: single and double substitutions of the spin-flip
+    window up to ci_level, each spin separately and combined."""
+    singles = _singles(nb - sf_level, nb, na, na + sf_level)
+    if sf_level == 2 and istate == 2:
+        excluded = _singles(nb - 1, nb, na, na + 1)
+        singles = [s for s in singles if s not in excluded]
+    a1 = [_excite(alpha, s) for s in singles]
+    b1 = [_excite(beta, s) for s in singles]
+    a2, b2 = [], []
+    if sf_level > 1:
+        for d in _doubles(nb - sf_level, nb, na, na + sf_level):
+            a2.append(_excite2(alpha, d))
+            b2.append(_excite2(beta, d))
+    out = []
+    if ci_level > 0:
+        out += [[istate, a, beta] for a in a1] + [[istate, alpha, b] for b in b1]
+    if ci_level > 1:
+        out += [[istate, a, b] for a in a1 for b in b1]
+        out += [[istate, a, beta] for a in a2] + [[istate, alpha, b] for b in b2]
+    if ci_level > 2:
+        out += [[istate, a, b] for a in a2 for b in b1] + [[istate, a, b] for a in a1 for b in b2]
+    if ci_level > 3:
+        out += [[istate, a, b] for a in a2 for b in b2]
+    return out
+
+
+EXCITATION_ALIASES = {"CUSTOM-SINGLES": "CUSTOM-SINGLE", "DOUBLES-PAIRED": "DOUBLE-PAIRED", "SINGLE": "S",
+                      "SINGLES": "S", "DOUBLE": "D", "DOUBLES": "D", "SINGLE-DOUBLE": "SD", "SINGLES-DOUBLES": "SD",
+                      "SPIN-FLIP-SINGLE": "SFS", "SPIN-FLIP-SINGLES": "SFS", "SF-S": "SFS",
+                      "SPIN-FLIP-DOUBLE": "SFD", "SPIN-FLIP-DOUBLES": "SFD", "SF-D": "SFD",
+                      "SPIN-FLIP-SINGLE-DOUBLE": "SFSD", "SPIN-FLIP-SINGLES-DOUBLES": "SFSD", "SF-SD": "SFSD"}
+EXCITATION_TYPES = {None, "HOMO-LUMO", "CUSTOM-SINGLE", "CUSTOM-PAIRED", "S", "D", "SD", "DOUBLE-PAIRED",
+                    "SFS", "SFD", "SFSD", "SFS-CISD", "SFD-CISD", "SFD-CISDT", "SFD-CISDTQ", "SFSD-CISD",
+                    "SFSD-CISDT", "SFSD-CISDTQ"}
+
+
+def excited_states(na, nb, norb, excitations=None, n_core=0, alpha_excitations=None, beta_excitations=None):
+    """Hartree-Fock state occupancies and spin-flip determinant list of
+    Util/structures.py:526-657 (set_excitations).
+
+    Returns (states, spin_flip): states is a list of (alpha, beta) occupancy lists,
+    ground state first; spin_flip a list of [state index, alpha, beta] (empty unless a
+    spin-flip type).  ``excitations`` takes the upstream keywords and aliases
+    (Util/structures.py:393-413); CUSTOM-SINGLE / CUSTOM-PAIRED come from
+    alpha_excitations / beta_excitations lists of [from, to] pairs."""
+    exc = excitations.upper() if isinstance(excitations, str) else excitations
+    exc = EXCITATION_ALIASES.get(exc, exc)
+    if exc is None and (alpha_excitations or beta_excitations):
+        exc = "CUSTOM-PAIRED" if (alpha_excitations and beta_excitations) else "CUSTOM-SINGLE"
+    if exc not in EXCITATION_TYPES:
+        raise ValueError("excitation type %r not recognised" % (excitations,))
+    alpha_g = [1] * na + [0] * (norb - na)
+    beta_g = [1] * nb + [0] * (norb - nb)
+    states = [(list(alpha_g), list(beta_g))]
+    if exc is None:
+        return states, []
+    spin_flip = []
+    a_ex = b_ex = a_dbl = b_dbl = []
+    if exc == "DOUBLE-PAIRED":
+        a_ex = _singles(n_core, nb, na, norb)
+    elif exc == "HOMO-LUMO":
+        a_ex = _singles(na - 1, na, na, na + 1)
+    elif exc in ("S", "D", "SD"):
+        a_ex, b_ex = _singles(n_core, na, na, norb), _singles(n_core, nb, nb, norb)
+        a_dbl, b_dbl = _doubles(n_core, na, na, norb), _doubles(n_core, nb, nb, norb)
+    elif exc.startswith("CUSTOM"):
+        a_ex = alpha_excitations or [[]]
+        b_ex = beta_excitations or [[]]
+    if "SF" in exc:
+        spin_flip = [[0, list(alpha_g), list(beta_g)]]
+        ao, bo = list(alpha_g), list(beta_g)
+        ci_level = 4 if "CISDTQ" in exc else 3 if "CISDT" in exc else 2 if "CISD" in exc else 1 if "CIS" in exc else 0
+        ao[na], bo[nb - 1] = 1, 0
+        if "SFS" in exc:
+            states.append((list(ao), list(bo)))
+            if "CI" in exc:
+                spin_flip += _ci_states(alpha_g, beta_g, na, nb, min(ci_level, 2), 1, 1)
+            else:
+                spin_flip += _spinflip_states(alpha_g, beta_g, na, nb, 1, 1)
+        if ao[-1] == 0:
+            ao[na + 1], bo[nb - 2] = 1, 0
+        if "SFSD" in exc:
+            states.append((list(ao), list(bo)))
+            if "CI" in exc:
+                spin_flip += _ci_states(alpha_g, beta_g, na, nb, ci_level, 2, 2)
+            else:
+                spin_flip += _spinflip_states(alpha_g, beta_g, na, nb, 2, 2)
+        if "SFD" in exc:
+            states.append((list(ao), list(bo)))
+            if "CI" in exc:
+                spin_flip += _ci_states(alpha_g, beta_g, na, nb, ci_level, 2, 1)
+            else:
+                spin_flip += _spinflip_states(alpha_g, beta_g, na, nb, 1, 1)
+                spin_flip += _spinflip_states(alpha_g, beta_g, na, nb, 2, 1)
+        return states, [[s[0], list(s[1]), list(s[2])] for s in spin_flip]
+    beta_o = beta_g
+    for i, ex in enumerate(a_ex):
+        if ex != []:
+            alpha_o = _excite(alpha_g, ex)
+        elif exc == "CUSTOM-PAIRED":
+            alpha_o, beta_o = alpha_g, _excite(beta_g, b_ex[i])
+        else:
+            break
+        if exc in ("S", "SD", "HOMO-LUMO"):
+            beta_o = beta_g
+        if exc == "DOUBLE-PAIRED":
+            beta_o = list(alpha_o)
+        states.append((list(alpha_o), list(beta_o)))
+    if exc in ("S", "SD"):
+        for ex in b_ex:
+            if ex == []:
+                break
+            states.append((list(alpha_g), _excite(beta_g, ex)))
+    if exc in ("D", "SD"):
+        for ea in a_ex:
+            for eb in b_ex:
+                states.append((_excite(alpha_g, ea), _excite(beta_g, eb)))
+        for ex in a_dbl:
+            states.append((_excite2(alpha_g, ex), list(beta_g)))
+        for ex in b_dbl:
+            states.append((list(alpha_g), _excite2(beta_g, ex)))
+    return states, []
+
+
+# ------------------------------------------------------------------------------------
+# Hartree-Fock states in the reference's order (pychem.py:62-93)
+# ------------------------------------------------------------------------------------
+def reorder_mos(C, occupancy):
+    """Util/structures.py:979-994: swap the newly occupied orbitals above the electron
+    count with the newly emptied ones below it, pairwise in order."""
+    n = sum(occupancy)
+    frm = [i for i in range(n) if occupancy[i] == 0]
+    to = [i for i in range(n, C.shape[1]) if occupancy[i] == 1]
+    C = C.clone()
+    for f, t in zip(frm, to):
+        C[:, [f, t]] = C[:, [t, f]]
+    return C
+
+
+def hf_states(engine, states, spin_flip=False, reference="UHF", constrain_excited=False, use_mom=True,
+              max_iter=300, e_tol=1e-10, d_tol=1e-8):
+    """SCF of every state (pychem.py:62-93, one basis set): for spin-flip lists the
+    highest-spin state first, otherwise the ground state first, from the core guess;
+    each later state starts from its predecessor's orbitals -- for a spin-flip state
+    with unequal spin occupancies both spins from the predecessor's alpha orbitals (with
+    the beta HOMO-region swaps of pychem.py:82-88 for unconstrained UHF), otherwise
+    reorder_mos of the predecessor's orbitals -- and, with use_mom, keeps them occupied
+    by maximum overlap (FIXED reference).  CUHF applies to every state for a CUHF
+    reference, and to the excited ones with constrain_excited (hartree_fock.py:99).
+    Returns one SCFResult per state, in state order."""
+    if reference not in ("UHF", "CUHF"):
+        raise ValueError("NOCI states need a UHF or CUHF reference")
+    mol = engine.mol
+    order = list(range(len(states)))
+    if spin_flip:
+        order.reverse()
+    out = [None] * len(states)
+
+    def run(idx, C0):
+        oa, ob = states[idx]
+        tot = [a + b for a, b in zip(oa, ob)]
+        constrained = reference == "CUHF" or (constrain_excited and idx != 0)
+        return uhf(engine, cuhf=constrained, max_iter=max_iter, e_tol=e_tol, d_tol=d_tol, C0=C0,
+                   mom=use_mom and C0 is not None, occ=(sum(oa), sum(ob)),
+                   cuhf_spaces=(tot.count(2), tot.count(1)))
+
+    out[order[0]] = run(order[0], None)
+    for k in range(1, len(order)):
+        idx, prev = order[k], order[k - 1]
+        oa, ob = states[idx]
+        pa, _ = states[prev]
+        C0 = None
+        if spin_flip and oa != ob:
+            Ca, Cb = out[prev].Ca.clone(), out[prev].Ca.clone()
+            keep = constrain_excited and idx != 0
+            if reference == "UHF" and not keep:
+                for s in range(sum(pa) - sum(oa)):
+                    t, f = sum(ob) - 1 + s, sum(pa) - 1 - s
+                    Cb[:, [f, t]] = Cb[:, [t, f]]
+            C0 = (Ca, Cb)
+        elif mol.NAlphaElectrons == sum(oa):
+            C0 = (reorder_mos(out[prev].Ca, oa), reorder_mos(out[prev].Cb, ob))
+        out[idx] = run(idx, C0)
+    return out
+
+
+def assemble(occupancy, C, hf_occupancy):
+    """Methods/noci.py:127-146: occupied columns of ``C`` (each must be occupied in its
+    Hartree-Fock state) first in order, the unoccupied ones after them."""
+    n = sum(occupancy)
+    cols = [None] * len(occupancy)
+    k_occ, k_virt = 0, n
+    for i, o in enumerate(occupancy):
+        if o == 0:
+            cols[k_virt] = i
+            k_virt += 1
+        elif o == 1 and hf_occupancy[i] == 1:
+            cols[k_occ] = i
+            k_occ += 1
+        else:
+            raise ValueError("spin-flip determinant needs an orbital its Hartree-Fock state leaves empty")
+    return C[:, cols]
+
+
+def determinants(states, results, spin_flip_list):
+    """NOCI determinants (alpha and beta orbitals): the Hartree-Fock states themselves,
+    or for spin-flip lists each entry's occupancies applied to the alpha orbitals of
+    its Hartree-Fock state for both spins (Methods/noci.py:149-173)."""
+    if not spin_flip_list:
+        return [r.Ca for r in results], [r.Cb for r in results]
+    da, db = [], []
+    for idx, oa, ob in spin_flip_list:
+        C, hf_occ = results[idx].Ca, states[idx][0]
+        da.append(assemble(oa, C, hf_occ))
+        db.append(assemble(ob, C, hf_occ))
+    return da, db
+
+
+# ------------------------------------------------------------------------------------
+# CI matrix (Methods/noci.py:51-109)
+# ------------------------------------------------------------------------------------
+def _pair(C1, C2, S, n):
+    """Batched Lowdin pairing (noci.py:183-205): C1, C2 (P, nbf, >= n)."""
+    A, B = C1[:, :, :n], C2[:, :, :n]
+    U, _, Vh = torch.linalg.svd(A.transpose(1, 2) @ S @ B)
+    A2, B2 = A @ U, B @ Vh.transpose(1, 2)
+    sign = torch.where((A2 * B2).sum(dim=1) < 0, -1.0, 1.0).to(B2.dtype)
+    return A2, B2 * sign.unsqueeze(1)
+
+
+def noci_matrix(engine, dets_a, dets_b, na, nb, return_pairs=False):
+    """CI Hamiltonian and overlap over the determinants (lower triangle with the
+    row's determinant as the bra, mirrored), as Methods/noci.py:55-106.  With
+    return_pairs, also the lower-triangle indices and the paired orbitals
+    (a1, a2, b1, b2), one row per pair."""
+    S, H = engine.S, engine.H
+    e_nuc = engine.mol.nuclear_repulsion()
+    m = len(dets_a)
+    ii, jj = torch.tril_indices(m, m).unbind(0)
+    Da, Db = torch.stack(dets_a), torch.stack(dets_b)
+    P = ii.numel()
+    dev = S.device
+    nbf = S.shape[0]
+    zeros_ab = torch.zeros(P, nbf, 0, dtype=torch.float64, device=dev)
+    a1, a2 = _pair(Da[ii], Da[jj], S, na) if na else (zeros_ab, zeros_ab)
+    b1, b2 = _pair(Db[ii], Db[jj], S, nb) if nb else (zeros_ab, zeros_ab)
+    ov_a = ((a1.transpose(1, 2) @ S) * a2.transpose(1, 2)).sum(dim=2)          # diag(a1^T S a2)
+    ov_b = ((b1.transpose(1, 2) @ S) * b2.transpose(1, 2)).sum(dim=2)
+    core_a = ((a1.transpose(1, 2) @ H) * a2.transpose(1, 2)).sum(dim=2)        # diag(a1^T H a2)
+    core_b = ((b1.transpose(1, 2) @ H) * b2.transpose(1, 2)).sum(dim=2)
+    s_state = ov_a.prod(dim=1) * ov_b.prod(dim=1)
+    keep_a, keep_b = ov_a > NOCI_THRESH, ov_b > NOCI_THRESH
+    one = torch.ones_like(ov_a)
+    reduced = torch.where(keep_a, ov_a, one).prod(dim=1) * torch.where(keep_b, ov_b, torch.ones_like(ov_b)).prod(dim=1)
+    # zero list in upstream order: alpha indices then beta indices
+    nz_a, nz_b = (~keep_a).sum(dim=1), (~keep_b).sum(dim=1)
+    first_a = torch.where(~keep_a, torch.arange(na, device=dev), na).min(dim=1).values if na else nz_a
+    first_b = torch.where(~keep_b, torch.arange(nb, device=dev), nb).min(dim=1).values if nb else nz_b
+    host = torch.stack([nz_a, nz_b, first_a, first_b], dim=1).cpu().tolist()
+    # co-densities: weighted (zero or one zero) or the first zero's pair densities (two zeros)
+    inv_a = torch.where(keep_a, 1.0 / torch.where(keep_a, ov_a, one), torch.zeros_like(ov_a))
+    inv_b = torch.where(keep_b, 1.0 / torch.where(keep_b, ov_b, torch.ones_like(ov_b)), torch.zeros_like(ov_b))
+    Wa = (a1 * inv_a.unsqueeze(1)) @ a2.transpose(1, 2)
+    Wb = (b1 * inv_b.unsqueeze(1)) @ b2.transpose(1, 2)
+    kind = []
+    Pa = torch.zeros(P, nbf, nbf, dtype=torch.float64, device=dev)
+    Pb = torch.zeros_like(Pa)
+    for p, (za, zb, fa, fb) in enumerate(host):
+        nz = za + zb
+        kind.append(min(nz, 3))
+        if nz == 1 or nz == 2:
+            z = fa if za else fb
+            spin_a = za > 0
+            if nz == 2:
+                if z < na:
+                    Pa[p] = torch.outer(a1[p, :, z], a2[p, :, z])
+                if z < nb:
+                    Pb[p] = torch.outer(b1[p, :, z], b2[p, :, z])
+            elif spin_a:
+                Pa[p] = torch.outer(a1[p, :, z], a2[p, :, z])
+            else:
+                Pb[p] = torch.outer(b1[p, :, z], b2[p, :, z])
+            if nz == 2:
+                Wa[p], Wb[p] = Pa[p], Pb[p]
+    need = [p for p in range(P) if kind[p] < 3]
+    elem = torch.zeros(P, dtype=torch.float64, device=dev)
+    if need:
+        idx = torch.tensor(need, device=dev)
+        J, K = engine.coulomb_exchange(torch.cat([Wa[idx], Wb[idx]]))
+        q = len(need)
+        Jt = J[:q] + J[q:]
+        Xa, Xb = -K[:q], -K[q:]
+        wa, wb = Wa[idx], Wb[idx]
+        kd = torch.tensor([kind[p] for p in need], device=dev)
+        e0 = 0.5 * (((wa + wb) * Jt).sum(dim=(1, 2)) + (wa * Xa).sum(dim=(1, 2)) + (wb * Xb).sum(dim=(1, 2)))
+        e0 = e0 + torch.where(keep_a[idx], core_a[idx] * inv_a[idx], torch.zeros_like(core_a[idx])).sum(dim=1)
+        e0 = e0 + torch.where(keep_b[idx], core_b[idx] * inv_b[idx], torch.zeros_like(core_b[idx])).sum(dim=1)
+        # one or two zeros: the active pair density against J and the active spin's exchange
+        za = torch.tensor([host[p][0] > 0 for p in need], device=dev)
+        Pact = torch.where(za.view(-1, 1, 1), Pa[idx], Pb[idx])
+        Xact = torch.where(za.view(-1, 1, 1), Xa, Xb)
+        e12 = (Pact * Jt).sum(dim=(1, 2)) + (Pact * Xact).sum(dim=(1, 2))
+        add = torch.zeros(q, dtype=torch.float64, device=dev)
+        for k, p in enumerate(need):
+            za_, zb_, fa_, fb_ = host[p]
+            if za_ + zb_ == 1:
+                add[k] = core_a[p, fa_] if za_ else core_b[p, fb_]
+        e12 = e12 + add
+        elem[idx] = torch.where(kd == 0, e0, e12)
+    hval = elem * reduced + e_nuc * s_state
+    Hci = torch.zeros(m, m, dtype=torch.float64, device=dev)
+    Sci = torch.zeros_like(Hci)
+    Hci[ii, jj] = hval
+    Hci[jj, ii] = hval
+    Sci[ii, jj] = s_state
+    Sci[jj, ii] = s_state
+    if return_pairs:
+        return Hci, Sci, (ii, jj, a1, a2, b1, b2)
+    return Hci, Sci
+
+
+def generalized_eigh(Hci, Sci):
+    """Solutions of H v = E S v with v^T S v = 1, ascending E: S = L L^T, the FP64
+    eigensolver on L^-1 H L^-T, v = L^-T y."""
+    L = torch.linalg.cholesky(Sci)
+    Li = torch.linalg.solve_triangular(L, torch.eye(L.shape[0], dtype=L.dtype, device=L.device), upper=False)
+    A = Li @ Hci @ Li.T
+    e, Y = eigen.eigh(0.5 * (A + A.T))
+    return e, Li.T @ Y
+
+
+def run(engine, excitations, reference="UHF", constrain_excited=False, max_iter=300, e_tol=1e-10, d_tol=1e-8):
+    """The whole NOCI calculation of Methods/noci.py:51-122 after pychem.py:62-93:
+    states, their SCFs, determinants, CI matrix and energies.  Returns a dict with
+    ``states`` (occupancies), ``hf`` (SCFResults), ``energies``, ``vectors``, ``H``,
+    ``S``."""
+    mol = engine.mol
+    na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+    states, sf = excited_states(na, nb, engine.nbf, excitations,
+                                n_core=n_core_orbitals([N_ELECTRONS[a[0]] for a in mol.atoms]))
+    spin_flip = isinstance(excitations, str) and "SF" in EXCITATION_ALIASES.get(excitations.upper(),
+                                                                                excitations.upper())
+    res = hf_states(engine, states, spin_flip=spin_flip, reference=reference, constrain_excited=constrain_excited,
+                    max_iter=max_iter, e_tol=e_tol, d_tol=d_tol)
+    dets_a, dets_b = determinants(states, res, sf if spin_flip else [])
+    Hci, Sci = noci_matrix(engine, dets_a, dets_b, na, nb)
+    e, v = generalized_eigh(Hci, Sci)
+    return dict(states=states, spin_flip=sf, hf=res, dets_alpha=dets_a, dets_beta=dets_b, energies=e, vectors=v,
+                H=Hci, S=Sci)

@@ -319,7 +319,16 @@ def mom_order(C, e, C_ref, n, S):
     return C[:, order], e[order]
 
 
-def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=False):
+def _sort_occupied(C, e, n):
+    """The first n columns ordered by energy, the rest kept (Util/structures.py:923-929)."""
+    if n > 1:
+        idx = torch.cat([torch.argsort(e[:n], stable=True), torch.arange(n, e.shape[0], device=e.device)])
+        C, e = C[:, idx], e[idx]
+    return C, e
+
+
+def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=False, occ=None,
+        cuhf_spaces=None):
     """Unrestricted (cuhf=False) or constrained unrestricted Hartree-Fock on a prepared
     GpuEngine, along Methods/hartree_fock.py:23-142: core-Hamiltonian guess for both
     spins, Fock matrices from pcg_digest_class_u, the CUHF constraint of
@@ -329,10 +338,15 @@ def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=
     matrices of the current densities.  C0 = (Ca, Cb): starting orbitals, occupied
     columns first (an excited determinant) instead of the core guess; mom: occupy by
     maximum overlap with C0's occupied orbitals (the FIXED reference of
-    Methods/hf_extensions/mom.py) instead of aufbau.  Returns SCFResult with E, Ca, Cb,
-    ea, eb, Da, Db, iterations, converged."""
+    Methods/hf_extensions/mom.py) instead of aufbau, the occupied orbitals then sorted
+    by energy (Util/structures.py:923-929).  occ = (n_alpha, n_beta) for a state other
+    than the molecule's own; cuhf_spaces = (core, active) counts of the constraint
+    (doubly and singly occupied positions of the state's occupancy lists,
+    hartree_fock.py:361-365), default (n_beta, n_alpha - n_beta).  Returns SCFResult
+    with E, Ca, Cb, ea, eb, Da, Db, iterations, converged."""
     mol = engine.mol
-    na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+    na, nb = occ if occ is not None else (mol.NAlphaElectrons, mol.NBetaElectrons)
+    ncore, nact = cuhf_spaces if cuhf_spaces is not None else (nb, na - nb)
     S, H = engine.S, engine.H
     dev = S.device
     e_nuc = mol.nuclear_repulsion()
@@ -353,7 +367,7 @@ def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=
         Cno = Shi @ V
         back = V.T @ Sh                             # Cno^-1
         order = torch.argsort(vals, descending=True)
-        core, virt = order[:nb], order[na:]
+        core, virt = order[:ncore], order[ncore + nact:]
         delta = Cno.T @ (0.5 * (Fa - Fb)) @ Cno
         lam = torch.zeros_like(delta)
         lam[core.unsqueeze(1), virt.unsqueeze(0)] = -delta[core.unsqueeze(1), virt.unsqueeze(0)]
@@ -406,8 +420,8 @@ def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=
     ea, Ca = diag(Fa)
     eb, Cb = diag(Fb)
     if mom:
-        Ca, ea = mom_order(Ca, ea, C0[0], na, S)
-        Cb, eb = mom_order(Cb, eb, C0[1], nb, S)
+        Ca, ea = _sort_occupied(*mom_order(Ca, ea, C0[0], na, S), na)
+        Cb, eb = _sort_occupied(*mom_order(Cb, eb, C0[1], nb, S), nb)
     return SCFResult(E=E, Ca=Ca, Cb=Cb, ea=ea, eb=eb, Da=Da, Db=Db, Fa=Fa, Fb=Fb, iterations=it,
                      converged=converged)
 

@@ -117,6 +117,9 @@ _EDITS = {
     "Methods/hf_extensions/diis.py": [("xrange", "range")],
     "Methods/basis_fit.py": [("xrange", "range")],
     "pychem.py": [("SafeConfigParser", "ConfigParser")],
+    # numpy.product was removed in NumPy 2
+    "Methods/noci.py": [("np.product(alpha_overlaps) * np.product(beta_overlaps)",
+                         "np.prod(alpha_overlaps) * np.prod(beta_overlaps)")],
 }
 
 _INITS = {

@@ -1,0 +1,173 @@
+"""NOCI on CPU: the oracle pinned to the reference's CI matrices, and the host logic of
+pychem_gb300.noci (state lists, spin-flip determinants, CI-matrix assembly with a dense
+einsum standing in for the GPU digestion) against the same fixtures.
+
+Fixtures: tests/golden/noci_*.npz from make_golden_noci.py.  Elements with two zero
+overlaps in one spin depend on the SVD's basis inside a degenerate null space
+(Methods/noci.py:279-300 takes the first zero's pair); they are compared against the
+oracle evaluated on the same paired orbitals instead of the reference's value.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle
+from pychem_gb300 import noci
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CASES = sorted(glob.glob(os.path.join(HERE, "golden", "noci_*.npz")))
+NAMES = [os.path.basename(c)[:-4] for c in CASES]
+
+
+def load(name):
+    return np.load(os.path.join(HERE, "golden", name + ".npz"))
+
+
+def basis_dependent(z):
+    """Mask of CI elements with two zero overlaps in one spin (reference pairing)."""
+    na, nb = int(z["n_alpha"]), int(z["n_beta"])
+    m = len(z["det_alpha"])
+    mask = np.zeros((m, m), dtype=bool)
+    for i in range(m):
+        for j in range(i + 1):
+            a1, a2 = oracle.noci_biorthogonalize(z["det_alpha"][i], z["det_alpha"][j], z["S"], na)
+            b1, b2 = oracle.noci_biorthogonalize(z["det_beta"][i], z["det_beta"][j], z["S"], nb)
+            za, zb = oracle.noci_zero_counts(a1, a2, b1, b2, z["S"])
+            mask[i, j] = mask[j, i] = za >= 2 or zb >= 2
+    return mask
+
+
+def test_fixtures_present():
+    assert len(CASES) >= 7
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_noci_matches_reference(name):
+    z = load(name)
+    e, v, H, S = oracle.noci(list(z["det_alpha"]), list(z["det_beta"]), z["S"], z["H"], z["eri_dense"],
+                             int(z["n_alpha"]), int(z["n_beta"]), float(z["E_nuc"]))
+    mask = basis_dependent(z)
+    assert np.abs(S - z["ci_S"]).max() < 1e-12
+    assert np.abs(np.where(mask, 0.0, H - z["ci_H"])).max() < 1e-9
+    if not mask.any():
+        assert np.abs(e - z["noci_energies"]).max() < 1e-9
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_assemble_matches_reference(name):
+    z = load(name)
+    for k, (idx, oa, ob) in enumerate(zip(z["sf_index"], z["sf_alpha"], z["sf_beta"])):
+        C, occ = z["hf_alpha"][idx], z["hf_occ_alpha"][idx]
+        assert np.array_equal(oracle.noci_assemble(oa, C, occ), z["det_alpha"][k])
+        assert np.array_equal(oracle.noci_assemble(ob, C, occ), z["det_beta"][k])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_state_lists_match_reference(name):
+    z = load(name)
+    na, nb, norb = int(z["n_alpha"]), int(z["n_beta"]), z["S"].shape[0]
+    states, sf = noci.excited_states(na, nb, norb, str(z["excitations"]))
+    assert [s[0] for s in states] == z["hf_occ_alpha"].tolist()
+    assert [s[1] for s in states] == z["hf_occ_beta"].tolist()
+    assert [s[0] for s in sf] == z["sf_index"].tolist()
+    assert [s[1] for s in sf] == z["sf_alpha"].tolist()
+    assert [s[2] for s in sf] == z["sf_beta"].tolist()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_determinants_match_reference(name):
+    z = load(name)
+    na, nb, norb = int(z["n_alpha"]), int(z["n_beta"]), z["S"].shape[0]
+    states, sf = noci.excited_states(na, nb, norb, str(z["excitations"]))
+
+    class R:
+        pass
+    res = []
+    for k in range(len(states)):
+        r = R()
+        r.Ca, r.Cb = torch.tensor(z["hf_alpha"][k]), torch.tensor(z["hf_beta"][k])
+        res.append(r)
+    da, db = noci.determinants(states, res, sf)
+    assert len(da) == len(z["det_alpha"])
+    for a, b, ra, rb in zip(da, db, z["det_alpha"], z["det_beta"]):
+        assert torch.equal(a, torch.tensor(ra)) and torch.equal(b, torch.tensor(rb))
+
+
+class _Mol:
+    def __init__(self, e):
+        self.e = e
+
+    def nuclear_repulsion(self):
+        return self.e
+
+
+class DenseEngine:
+    """CPU stand-in for GpuEngine in the CI-matrix assembly: S, H and J/K by einsum on
+    the fixture's dense ERI tensor."""
+
+    def __init__(self, z):
+        self.S, self.H = torch.tensor(z["S"]), torch.tensor(z["H"])
+        self.eri = torch.tensor(z["eri_dense"])
+        self.mol = _Mol(float(z["E_nuc"]))
+        self.nbf = self.S.shape[0]
+
+    def coulomb_exchange(self, W):
+        return torch.einsum("ncd,abcd->nab", W, self.eri), torch.einsum("ncb,abcd->nad", W, self.eri)
+
+
+def check_ci_matrix(z, H, S, pairs, tol):
+    """H, S against the reference outside basis-dependent elements, and every element
+    against the oracle on the same paired orbitals."""
+    na, nb = int(z["n_alpha"]), int(z["n_beta"])
+    mask = basis_dependent(z)
+    H, S = H.cpu().numpy(), S.cpu().numpy()
+    assert np.abs(S - z["ci_S"]).max() < 1e-12
+    assert np.abs(np.where(mask, 0.0, H - z["ci_H"])).max() < tol
+    ii, jj, a1, a2, b1, b2 = [t.cpu().numpy() for t in pairs]
+    for p in range(len(ii)):
+        h, s = oracle.noci_element_paired(a1[p], a2[p], b1[p], b2[p], z["S"], z["H"], z["eri_dense"], na, nb,
+                                          float(z["E_nuc"]))
+        assert abs(h - H[ii[p], jj[p]]) < tol, (ii[p], jj[p])
+        assert abs(s - S[ii[p], jj[p]]) < 1e-12
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_ci_matrix_assembly(name):
+    z = load(name)
+    dets_a = [torch.tensor(x) for x in z["det_alpha"]]
+    dets_b = [torch.tensor(x) for x in z["det_beta"]]
+    H, S, pairs = noci.noci_matrix(DenseEngine(z), dets_a, dets_b, int(z["n_alpha"]), int(z["n_beta"]),
+                                   return_pairs=True)
+    check_ci_matrix(z, H, S, pairs, 1e-9)
+
+
+def test_core_orbital_counts():
+    assert noci.n_core_orbitals([3, 1]) == 1
+    assert noci.n_core_orbitals([8, 1, 1]) == 1
+    assert noci.n_core_orbitals([17, 11]) == 10
+    assert noci.n_core_orbitals([1, 2]) == 0
+
+
+def test_excitation_lists():
+    # HOMO-LUMO adds one alpha single; S adds every single of each spin above the core
+    states, sf = noci.excited_states(3, 3, 6, "HOMO-LUMO")
+    assert states == [([1, 1, 1, 0, 0, 0], [1, 1, 1, 0, 0, 0]), ([1, 1, 0, 1, 0, 0], [1, 1, 1, 0, 0, 0])]
+    assert sf == []
+    states, _ = noci.excited_states(2, 2, 4, "SINGLES", n_core=1)
+    assert len(states) == 1 + 2 + 2
+    assert states[1] == ([1, 0, 1, 0], [1, 1, 0, 0])
+    states, _ = noci.excited_states(2, 2, 4, "SD", n_core=0)
+    # 4 + 4 singles, 16 alpha x beta pairs, one double per spin
+    assert len(states) == 1 + 8 + 16 + 2
+    with pytest.raises(ValueError):
+        noci.excited_states(2, 2, 4, "TRIPLES")
+
+
+def test_reorder_mos():
+    C = torch.arange(16.0).view(4, 4)
+    out = noci.reorder_mos(C, [1, 0, 1, 0])
+    assert torch.equal(out[:, 1], C[:, 2]) and torch.equal(out[:, 2], C[:, 1])
+    assert torch.equal(noci.reorder_mos(C, [1, 1, 0, 0]), C)
