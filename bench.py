@@ -353,6 +353,64 @@ def alkane_leg(torch, args):
     return out
 
 
+def noci_leg(torch, args):
+    """Spin-flip NOCI (Methods/noci.py) on twisted ethylene / 6-31G with SFD-CISD
+    determinants: the state SCFs in the reference's order (high spin first), the
+    spin-flip determinants, the CI matrix over every determinant pair (J/K of all
+    co-densities in one batched digestion per integral class) and the generalised
+    eigenproblem.  cpu_noci_matrix_s: the oracle's CI matrix (numpy, dense ERI einsums,
+    one core) on a bounded sample of the same pairs, extrapolated to all of them."""
+    import numpy as np
+    from pychem_gb300 import noci
+    from pychem_gb300 import workloads as W
+    from pychem_gb300.engine import GpuEngine
+    from pychem_gb300.molecule import Molecule
+    from oracle import oracle
+    mol = Molecule(W.twisted_ethylene(90.0), "6-31G")
+    exc = "SFD-CISD"
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng = GpuEngine(mol).prepare()
+    out = noci.run(eng, exc, reference="UHF", constrain_excited=True)
+    torch.cuda.synchronize()
+    t_total = time.perf_counter() - t0
+    na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+    da, db = out["dets_alpha"], out["dets_beta"]
+    m = len(da)
+    ts = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        Hci, Sci = noci.noci_matrix(eng, da, db, na, nb)
+        noci.generalized_eigh(Hci, Sci)
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b) / 1e3)
+    t_ci = min(ts)
+    npairs = m * (m + 1) // 2
+    # CPU: the oracle on a bounded sample of pairs
+    S, H = eng.S.cpu().numpy(), eng.H.cpu().numpy()
+    eri = eng.dense_eri().cpu().numpy()
+    e_nuc = mol.nuclear_repulsion()
+    Da = [x.cpu().numpy() for x in da]
+    Db = [x.cpu().numpy() for x in db]
+    pairs = [(i, j) for i in range(m) for j in range(i + 1)]
+    rng = np.random.default_rng(SEED)
+    sample = [pairs[k] for k in rng.choice(len(pairs), size=min(24, len(pairs)), replace=False)]
+    c0 = time.perf_counter()
+    for i, j in sample:
+        oracle.noci_element(Da[i], Db[i], Da[j], Db[j], S, H, eri, na, nb, e_nuc)
+    cpu_per_pair = (time.perf_counter() - c0) / len(sample)
+    e = out["energies"].cpu().numpy()
+    return {"workload": "C2H4 twisted 90 deg, 6-31G (%d AO), %s: %d determinants, %d pairs" % (eng.nbf, exc, m, npairs),
+            "ttc_s": t_total, "ci_matrix_and_eigh_s": t_ci, "pairs_per_s": npairs / t_ci,
+            "hf_state_energies": [r.E for r in out["hf"]], "hf_iterations": [r.iterations for r in out["hf"]],
+            "noci_lowest": [float(x) for x in e[:3]],
+            "cpu_noci_matrix_s": cpu_per_pair * npairs, "cpu_sample_pairs": len(sample), "cpu_cores": 1,
+            "ci_speedup_vs_cpu_oracle": cpu_per_pair * npairs / t_ci}
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -470,6 +528,7 @@ def gpu_arm(args):
     ens = ensemble_leg(torch, args) if world == 1 or rank == 0 else None
     alk = alkane_leg(torch, args) if world == 1 or rank == 0 else None
     lrn = learned_leg(torch, args) if world == 1 or rank == 0 else None
+    nci = noci_leg(torch, args) if world == 1 or rank == 0 else None
 
     # max over ranks
     if world > 1:
@@ -520,6 +579,7 @@ def gpu_arm(args):
         "ensemble": ens,
         "alkane_mixed": alk,
         "learned_guess": lrn,
+        "noci_spin_flip": nci,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": out["h2d_bytes"],
                 "d2h_bytes_per_step": out["d2h_bytes"]},
         "gpu_launches": launches,

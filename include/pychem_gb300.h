@@ -207,6 +207,16 @@ int pcg_digest_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs
 int pcg_digest_class_u(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                        int ntask, const double *store, const double *Da, const double *Db, double *GJ,
                        double *GKa, double *GKb, void *stream);
+/* Co-density digestion for non-orthogonal CI (Methods/noci.py:243-300 evaluates
+ * hartree_fock.py:345-347 on the non-symmetric co-densities of Lowdin-paired
+ * determinants): nd densities W, consecutive nbf x nbf row-major blocks; per density
+ * GJ += the Coulomb part of (W + W^T)/2 and GK += both orientations of the exchange
+ * blocks, so that J[W] = (GJ + GJ^T)/4 and K[W] = -GK/2 with
+ * J_ab = sum_cd (ab|cd) W_cd, K_ad = sum_bc (ab|cd) W_cb.  One molecule (no
+ * ensemble block table). */
+int pcg_digest_class_co(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
+                        int ntask, const double *store, int nd, const double *W, double *GJ, double *GK,
+                        void *stream);
 int pcg_fock_build(int n, const double *H, const double *G, double *F, void *stream);
 /* Same for nblocks consecutive ld x ld blocks (an ensemble of molecules). */
 int pcg_fock_build_batched(int nblocks, int ld, const double *H, const double *G, double *F, void *stream);

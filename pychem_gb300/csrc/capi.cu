@@ -133,6 +133,17 @@ int pcg_digest_class_u(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pai
                              GKb, (cudaStream_t)stream);
 }
 
+int pcg_digest_class_co(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                        const double* store, int nd, const double* W, double* GJ, double* GK, void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs || nd < 0 || (nd > 0 && (!W || !GJ || !GK))) {
+    pcg_set_error("pcg_digest_class_co: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  if (basis->sh_blk) { pcg_set_error("pcg_digest_class_co: one molecule only"); return PCG_ERR_UNSUPPORTED; }
+  return pcg_launch_digest_co(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, nd, W, GJ, GK,
+                              (cudaStream_t)stream);
+}
+
 int pcg_fock_build(int n, const double* H, const double* G, double* F, void* stream) {
   return pcg_launch_fock(n, H, G, F, (cudaStream_t)stream);
 }

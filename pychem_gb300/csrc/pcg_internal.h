@@ -41,6 +41,8 @@ int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const i
 int pcg_launch_digest_u(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                         const double* store, const double* Da, const double* Db, double* GJ, double* GKa,
                         double* GKb, cudaStream_t s);
+int pcg_launch_digest_co(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
+                         const double* store, int nd, const double* W, double* GJ, double* GK, cudaStream_t s);
 int pcg_launch_dense(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                      const double* store, double* eri, cudaStream_t s);
 

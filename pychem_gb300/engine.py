@@ -377,27 +377,21 @@ class GpuEngine:
         (nd, nbf, nbf): J_ab = sum_cd (ab|cd) W_cd, K_ad = sum_bc (ab|cd) W_cb
         (Methods/hartree_fock.py:345-347, applied by Methods/noci.py:261-318).
 
-        The unrestricted digestion is linear in each density and accumulates, per
-        unique quartet, one orientation of each exchange block (G[M]_ad from M_bc and
-        so on); with (D_a, D_b) = (W, W^T) its exchange buffers hold G[W] and G[W^T],
-        and K[W] = -(G[W^T] + G[W]^T) / 2 reproduces all eight index permutations.  The
-        Coulomb buffer sees (W + W^T) / 2, which is all J depends on."""
-        n = self.nbf
+        One pcg_digest_class_co launch per class part digests every density (blockIdx.y
+        selects it).  Per unique quartet the digestion accumulates one orientation of
+        each exchange block (G[M]_ad from M_bc and so on); the kernel adds G[W^T] and
+        G[W]^T, which together hold all eight index permutations: K[W] = -GK/2.  The
+        Coulomb buffer sees (W + W^T)/2, all that J depends on: J = (GJ + GJ^T)/4."""
+        W = W.contiguous()
         nd = W.shape[0]
-        J = torch.empty_like(W)
-        K = torch.empty_like(W)
-        G = torch.zeros(3, n, n, dtype=torch.float64, device=self.dev)
-        for d in range(nd):
-            Wd, Wt = W[d].contiguous(), W[d].T.contiguous()
-            G.zero_()
-            for cls, rec in self.classes.items():
-                for part, (tasks, ntask) in rec.items():
-                    _lib.call("pcg_digest_class_u", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
-                              _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), _ptr(Wd), _ptr(Wt), _ptr(G[0]),
-                              _ptr(G[1]), _ptr(G[2]), _stream())
-            J[d] = 0.25 * (G[0] + G[0].T)
-            K[d] = -0.5 * (G[2] + G[1].T)
-        return J, K
+        GJ = torch.zeros_like(W)
+        GK = torch.zeros_like(W)
+        for cls, rec in self.classes.items():
+            for part, (tasks, ntask) in rec.items():
+                _lib.call("pcg_digest_class_co", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
+                          _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), nd, _ptr(W), _ptr(GJ), _ptr(GK),
+                          _stream())
+        return 0.25 * (GJ + GJ.transpose(1, 2)), -0.5 * GK
 
     def dense_eri(self):
         """Dense nbf^4 tensor (8-fold symmetric fill), zero where screened out."""

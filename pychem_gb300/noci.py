@@ -337,85 +337,73 @@ def _pair(C1, C2, S, n):
 
 def noci_matrix(engine, dets_a, dets_b, na, nb, return_pairs=False):
     """CI Hamiltonian and overlap over the determinants (lower triangle with the
-    row's determinant as the bra, mirrored), as Methods/noci.py:55-106.  With
-    return_pairs, also the lower-triangle indices and the paired orbitals
+    row's determinant as the bra, mirrored), as Methods/noci.py:55-106, without a
+    host round trip: zero-overlap cases are masks, the first zero's orbital pair a
+    column gather, and the J/K of all pairs' co-densities one batched digestion.
+    With return_pairs, also the lower-triangle indices and the paired orbitals
     (a1, a2, b1, b2), one row per pair."""
     S, H = engine.S, engine.H
     e_nuc = engine.mol.nuclear_repulsion()
     m = len(dets_a)
-    ii, jj = torch.tril_indices(m, m).unbind(0)
-    Da, Db = torch.stack(dets_a), torch.stack(dets_b)
-    P = ii.numel()
     dev = S.device
-    nbf = S.shape[0]
-    zeros_ab = torch.zeros(P, nbf, 0, dtype=torch.float64, device=dev)
-    a1, a2 = _pair(Da[ii], Da[jj], S, na) if na else (zeros_ab, zeros_ab)
-    b1, b2 = _pair(Db[ii], Db[jj], S, nb) if nb else (zeros_ab, zeros_ab)
-    ov_a = ((a1.transpose(1, 2) @ S) * a2.transpose(1, 2)).sum(dim=2)          # diag(a1^T S a2)
-    ov_b = ((b1.transpose(1, 2) @ S) * b2.transpose(1, 2)).sum(dim=2)
-    core_a = ((a1.transpose(1, 2) @ H) * a2.transpose(1, 2)).sum(dim=2)        # diag(a1^T H a2)
-    core_b = ((b1.transpose(1, 2) @ H) * b2.transpose(1, 2)).sum(dim=2)
+    f64 = torch.float64
+    ii, jj = torch.tril_indices(m, m, device=dev).unbind(0)
+    Da, Db = torch.stack(dets_a), torch.stack(dets_b)
+    P, nbf = ii.numel(), S.shape[0]
+    empty = torch.zeros(P, nbf, 0, dtype=f64, device=dev)
+    a1, a2 = _pair(Da[ii], Da[jj], S, na) if na else (empty, empty)
+    b1, b2 = _pair(Db[ii], Db[jj], S, nb) if nb else (empty, empty)
+
+    def diag(x1, M, x2):                                     # diag(x1^T M x2) per pair
+        return ((x1.transpose(1, 2) @ M) * x2.transpose(1, 2)).sum(dim=2)
+
+    ov_a, ov_b = diag(a1, S, a2), diag(b1, S, b2)
+    core_a, core_b = diag(a1, H, a2), diag(b1, H, b2)
     s_state = ov_a.prod(dim=1) * ov_b.prod(dim=1)
     keep_a, keep_b = ov_a > NOCI_THRESH, ov_b > NOCI_THRESH
-    one = torch.ones_like(ov_a)
-    reduced = torch.where(keep_a, ov_a, one).prod(dim=1) * torch.where(keep_b, ov_b, torch.ones_like(ov_b)).prod(dim=1)
-    # zero list in upstream order: alpha indices then beta indices
+    inv_a = torch.where(keep_a, 1.0 / torch.where(keep_a, ov_a, 1.0), 0.0)
+    inv_b = torch.where(keep_b, 1.0 / torch.where(keep_b, ov_b, 1.0), 0.0)
+    reduced = torch.where(keep_a, ov_a, 1.0).prod(dim=1) * torch.where(keep_b, ov_b, 1.0).prod(dim=1)
     nz_a, nz_b = (~keep_a).sum(dim=1), (~keep_b).sum(dim=1)
-    first_a = torch.where(~keep_a, torch.arange(na, device=dev), na).min(dim=1).values if na else nz_a
-    first_b = torch.where(~keep_b, torch.arange(nb, device=dev), nb).min(dim=1).values if nb else nz_b
-    host = torch.stack([nz_a, nz_b, first_a, first_b], dim=1).cpu().tolist()
-    # co-densities: weighted (zero or one zero) or the first zero's pair densities (two zeros)
-    inv_a = torch.where(keep_a, 1.0 / torch.where(keep_a, ov_a, one), torch.zeros_like(ov_a))
-    inv_b = torch.where(keep_b, 1.0 / torch.where(keep_b, ov_b, torch.ones_like(ov_b)), torch.zeros_like(ov_b))
+    nz = nz_a + nz_b
+    # the zero list runs over alpha indices, then beta: its first entry
+    first_a = torch.where(~keep_a, torch.arange(na, device=dev), na).amin(dim=1) if na else nz_a
+    first_b = torch.where(~keep_b, torch.arange(nb, device=dev), nb).amin(dim=1) if nb else nz_b
+    spin_a = nz_a > 0
+    z = torch.where(spin_a, first_a, first_b)
+
+    def pair_density(x1, x2, n):                             # outer(x1[:, z], x2[:, z]), 0 where z >= n
+        if n == 0:
+            return torch.zeros(P, nbf, nbf, dtype=f64, device=dev), torch.zeros(P, dtype=torch.bool, device=dev)
+        idx = z.clamp(max=n - 1).view(P, 1, 1).expand(P, nbf, 1)
+        return x1.gather(2, idx) @ x2.gather(2, idx).transpose(1, 2), z < n
+
+    Pa, in_a = pair_density(a1, a2, na)
+    Pb, in_b = pair_density(b1, b2, nb)
+    one, two = nz == 1, nz == 2
+    Pa = Pa * ((two & in_a) | (one & spin_a)).view(P, 1, 1)
+    Pb = Pb * ((two & in_b) | (one & ~spin_a)).view(P, 1, 1)
     Wa = (a1 * inv_a.unsqueeze(1)) @ a2.transpose(1, 2)
     Wb = (b1 * inv_b.unsqueeze(1)) @ b2.transpose(1, 2)
-    kind = []
-    Pa = torch.zeros(P, nbf, nbf, dtype=torch.float64, device=dev)
-    Pb = torch.zeros_like(Pa)
-    for p, (za, zb, fa, fb) in enumerate(host):
-        nz = za + zb
-        kind.append(min(nz, 3))
-        if nz == 1 or nz == 2:
-            z = fa if za else fb
-            spin_a = za > 0
-            if nz == 2:
-                if z < na:
-                    Pa[p] = torch.outer(a1[p, :, z], a2[p, :, z])
-                if z < nb:
-                    Pb[p] = torch.outer(b1[p, :, z], b2[p, :, z])
-            elif spin_a:
-                Pa[p] = torch.outer(a1[p, :, z], a2[p, :, z])
-            else:
-                Pb[p] = torch.outer(b1[p, :, z], b2[p, :, z])
-            if nz == 2:
-                Wa[p], Wb[p] = Pa[p], Pb[p]
-    need = [p for p in range(P) if kind[p] < 3]
-    elem = torch.zeros(P, dtype=torch.float64, device=dev)
-    if need:
-        idx = torch.tensor(need, device=dev)
-        J, K = engine.coulomb_exchange(torch.cat([Wa[idx], Wb[idx]]))
-        q = len(need)
-        Jt = J[:q] + J[q:]
-        Xa, Xb = -K[:q], -K[q:]
-        wa, wb = Wa[idx], Wb[idx]
-        kd = torch.tensor([kind[p] for p in need], device=dev)
-        e0 = 0.5 * (((wa + wb) * Jt).sum(dim=(1, 2)) + (wa * Xa).sum(dim=(1, 2)) + (wb * Xb).sum(dim=(1, 2)))
-        e0 = e0 + torch.where(keep_a[idx], core_a[idx] * inv_a[idx], torch.zeros_like(core_a[idx])).sum(dim=1)
-        e0 = e0 + torch.where(keep_b[idx], core_b[idx] * inv_b[idx], torch.zeros_like(core_b[idx])).sum(dim=1)
-        # one or two zeros: the active pair density against J and the active spin's exchange
-        za = torch.tensor([host[p][0] > 0 for p in need], device=dev)
-        Pact = torch.where(za.view(-1, 1, 1), Pa[idx], Pb[idx])
-        Xact = torch.where(za.view(-1, 1, 1), Xa, Xb)
-        e12 = (Pact * Jt).sum(dim=(1, 2)) + (Pact * Xact).sum(dim=(1, 2))
-        add = torch.zeros(q, dtype=torch.float64, device=dev)
-        for k, p in enumerate(need):
-            za_, zb_, fa_, fb_ = host[p]
-            if za_ + zb_ == 1:
-                add[k] = core_a[p, fa_] if za_ else core_b[p, fb_]
-        e12 = e12 + add
-        elem[idx] = torch.where(kd == 0, e0, e12)
+    t2 = two.view(P, 1, 1)
+    Wa, Wb = torch.where(t2, Pa, Wa), torch.where(t2, Pb, Wb)
+    J, K = engine.coulomb_exchange(torch.cat([Wa, Wb]))
+    Jt, Xa, Xb = J[:P] + J[P:], -K[:P], -K[P:]
+
+    def inner(x, y):
+        return (x * y).sum(dim=(1, 2))
+
+    e0 = 0.5 * (inner(Wa + Wb, Jt) + inner(Wa, Xa) + inner(Wb, Xb))
+    e0 = e0 + (core_a * inv_a).sum(dim=1) + (core_b * inv_b).sum(dim=1)
+    sa = spin_a.view(P, 1, 1)
+    Pact, Xact = torch.where(sa, Pa, Pb), torch.where(sa, Xa, Xb)
+    e12 = inner(Pact, Jt) + inner(Pact, Xact)
+    zc_a = core_a.gather(1, first_a.clamp(max=max(na - 1, 0)).view(P, 1)).squeeze(1) if na else e12 * 0
+    zc_b = core_b.gather(1, first_b.clamp(max=max(nb - 1, 0)).view(P, 1)).squeeze(1) if nb else e12 * 0
+    e12 = e12 + torch.where(one, torch.where(spin_a, zc_a, zc_b), 0.0)
+    elem = torch.where(nz == 0, e0, torch.where(nz <= 2, e12, 0.0))
     hval = elem * reduced + e_nuc * s_state
-    Hci = torch.zeros(m, m, dtype=torch.float64, device=dev)
+    Hci = torch.zeros(m, m, dtype=f64, device=dev)
     Sci = torch.zeros_like(Hci)
     Hci[ii, jj] = hval
     Hci[jj, ii] = hval

@@ -83,6 +83,20 @@ def alkane(n=12, cc=1.54, ch=1.09, jitter=0.03, seed=2026):
     return [[a[0], a[1]] + list(map(float, p)) for a, p in zip(atoms, xyz)]
 
 
+def twisted_ethylene(twist=90.0, cc=1.34, ch=1.086, hch=117.0):
+    """C2H4 with one CH2 group rotated by ``twist`` degrees about the C=C axis (x): at
+    90 degrees the pi bond is broken and the singlet is a diradical, the textbook case
+    for spin-flip NOCI."""
+    half = math.radians(hch / 2.0)
+    out = [["C", 6.0, 0.0, 0.0, 0.0], ["C", 6.0, cc, 0.0, 0.0]]
+    for c_x, sign, rot in ((0.0, -1.0, 0.0), (cc, 1.0, math.radians(twist))):
+        for s in (1.0, -1.0):
+            y, z = ch * math.sin(half) * s, 0.0
+            y, z = y * math.cos(rot) - z * math.sin(rot), y * math.sin(rot) + z * math.cos(rot)
+            out.append(["H", 1.0, c_x + sign * ch * math.cos(half), y, z])
+    return out
+
+
 def _tetra_dirs():
     return np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], dtype=float) / math.sqrt(3.0)
 
