@@ -354,7 +354,7 @@ def alkane_leg(torch, args):
 
 
 def noci_leg(torch, args):
-    """Spin-flip NOCI (Methods/noci.py) on twisted ethylene / 6-31G with SFD-CISD
+    """Spin-flip NOCI (Methods/noci.py) on C2 (r = 1.25 A) / cc-pVDZ with SFD-CISD
     determinants: the state SCFs in the reference's order (high spin first), the
     spin-flip determinants, the CI matrix over every determinant pair (J/K of all
     co-densities in one batched digestion per integral class) and the generalised
@@ -362,11 +362,10 @@ def noci_leg(torch, args):
     one core) on a bounded sample of the same pairs, extrapolated to all of them."""
     import numpy as np
     from pychem_gb300 import noci
-    from pychem_gb300 import workloads as W
     from pychem_gb300.engine import GpuEngine
     from pychem_gb300.molecule import Molecule
     from oracle import oracle
-    mol = Molecule(W.twisted_ethylene(90.0), "6-31G")
+    mol = Molecule([["C", 6.0, 0.0, 0.0, 0.0], ["C", 6.0, 1.25, 0.0, 0.0]], "cc-pVDZ")
     exc = "SFD-CISD"
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -403,7 +402,7 @@ def noci_leg(torch, args):
         oracle.noci_element(Da[i], Db[i], Da[j], Db[j], S, H, eri, na, nb, e_nuc)
     cpu_per_pair = (time.perf_counter() - c0) / len(sample)
     e = out["energies"].cpu().numpy()
-    return {"workload": "C2H4 twisted 90 deg, 6-31G (%d AO), %s: %d determinants, %d pairs" % (eng.nbf, exc, m, npairs),
+    return {"workload": "C2 r=1.25 A, cc-pVDZ (%d AO), %s: %d determinants, %d pairs" % (eng.nbf, exc, m, npairs),
             "ttc_s": t_total, "ci_matrix_and_eigh_s": t_ci, "pairs_per_s": npairs / t_ci,
             "hf_state_energies": [r.E for r in out["hf"]], "hf_iterations": [r.iterations for r in out["hf"]],
             "noci_lowest": [float(x) for x in e[:3]],

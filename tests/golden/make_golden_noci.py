@@ -44,6 +44,7 @@ CASES = [
     ("noci_lih_sfd_cisd_sto3g", lih(2.1), "STO-3G", "SFD-CISD"),
     ("noci_lih_sfsd_cisd_sto3g", lih(1.9), "STO-3G", "SFSD-CISD"),
     ("noci_h2_homo_lumo_631g", h2(0.9), "6-31G", "HOMO-LUMO"),
+    ("noci_c2_sfd_cisd_631g", [["C", 6.0, 0.0, 0.0, 0.0], ["C", 6.0, 1.25, 0.0, 0.0]], "6-31G", "SFD-CISD"),
 ]
 
 
