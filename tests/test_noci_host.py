@@ -179,3 +179,21 @@ def test_reorder_mos():
     out = noci.reorder_mos(C, [1, 0, 1, 0])
     assert torch.equal(out[:, 1], C[:, 2]) and torch.equal(out[:, 2], C[:, 1])
     assert torch.equal(noci.reorder_mos(C, [1, 1, 0, 0]), C)
+
+
+def test_spin_flip_lists_without_ci_fail_like_the_reference():
+    """Upstream's plain SFD list names a third Hartree-Fock state that its state list
+    lacks (IndexError) and its SFSD list asks for orbitals the high-spin states leave
+    empty (ValueError in noci.assemble_orbitals); both fail the same way here."""
+    class R:
+        pass
+
+    for exc, err in (("SFD", IndexError), ("SFSD", ValueError)):
+        states, sf = noci.excited_states(2, 2, 6, exc)
+        res = []
+        for _ in states:
+            r = R()
+            r.Ca = r.Cb = torch.eye(6, dtype=torch.float64)
+            res.append(r)
+        with pytest.raises(err):
+            noci.determinants(states, res, sf)
