@@ -207,6 +207,14 @@ int pcg_digest_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs
 int pcg_digest_class_u(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                        int ntask, const double *store, const double *Da, const double *Db, double *GJ,
                        double *GKa, double *GKb, void *stream);
+/* Electron-scattering integrals (ab|j0(S r12)|cd) of one class for a task list, same
+ * store layout as pcg_eri_class (FP64): the operator of Methods/properties.py:20-23,
+ * fundamentals of Methods/c_ints/two_electron_scattering.c:6-81 with z^-m j_m(z) by
+ * the regimes of spherical_bessel_j.c:5-81.  S >= 0 is the momentum transfer in the
+ * reference's units (inverse bohr).  Used for the Schwarz pass (diagonal tasks) and
+ * the screened store of each grid value. */
+int pcg_scattering_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
+                         int ntask, double S, double *store, void *stream);
 /* Co-density digestion for non-orthogonal CI (Methods/noci.py:243-300 evaluates
  * hartree_fock.py:345-347 on the non-symmetric co-densities of Lowdin-paired
  * determinants): nd densities W, consecutive nbf x nbf row-major blocks; per density

@@ -26,6 +26,12 @@
  *                      (two_electron_contract.c:45), bra and ket HRR on contracted
  *                      integrals (two_electron_hrr.c:82), Cartesian normalisation and
  *                      Cartesian->spherical transform (integrals.py:541-547)
+ *   scattering ....... Methods/c_ints/two_electron_scattering.c:6-81 (the j0(S r12)
+ *                      operator of Methods/properties.py: fundamentals
+ *                      U_P U_Q exp(-S^2 (sigma_P + sigma_Q)/4) S^2m z^-m j_m(z),
+ *                      z = S |P - Q|, with its S = 0 and R = 0 cases), written here in
+ *                      the unscaled Obara-Saika form (an extra (2 rho)^-m); z^-m j_m
+ *                      by the piecewise scheme of spherical_bessel_j.c:5-81
  */
 #include <math.h>
 #include <stdlib.h>
@@ -306,6 +312,55 @@ int oracle_one_electron(const or_shell *sa, const or_shell *sb, int natom, const
 
 #define NE_MAX 35 /* cart_offset(5): all Cartesians with l <= 4 */
 
+/* Two-electron operator: 0 = 1/r12, 1 = j0(S r12) (electron scattering). */
+static int g_op = 0;
+static double g_S = 0.0;
+
+void oracle_set_operator(int op, double S) { g_op = op; g_S = S; }
+
+/* z^-m j_m(z), m = 0..lmax, by the regimes of spherical_bessel_j.c: the power series
+ * about 0 below z = 10 (1, 3, 6 or 20 terms by the size of z), the two-term
+ * asymptotic form above 100, upward recursion from j0 and j1 between; values below
+ * 1e-16 in magnitude set to 0. */
+void oracle_sph_bessel(int lmax, double z, double *j)
+{
+    if (z < 10.0) {
+        int kmax = z < 1e-3 ? 1 : (z < 1e-1 ? 3 : (z < 1.0 ? 6 : 20));
+        double z2 = z * z, df = 1.0;
+        for (int m = 0; m <= lmax; ++m) {
+            df *= (double)(2 * m + 1);
+            double sum = 1.0, odd = (double)(2 * m + 1), oddprod = 1.0, zp = 1.0, den = 1.0, sg = 1.0;
+            for (int k = 1; k <= kmax; ++k) {
+                odd += 2.0;
+                oddprod *= odd;
+                zp *= z2;
+                sg = -sg;
+                den *= 2.0 * k;
+                sum += sg * zp / (den * oddprod);
+            }
+            j[m] = sum / df;
+        }
+    } else if (z > 100.0) {
+        double zi = 1.0 / z, zi2 = zi * zi, zm = 1.0, shift = z;
+        j[0] = sin(z) * zi;
+        for (int m = 1; m <= lmax; ++m) {
+            double c = (double)(m * (m + 1) / 2);
+            zm *= zi;
+            shift -= 0.5 * M_PI;
+            j[m] = zm * (zi * sin(shift) + c * zi2 * cos(shift));
+        }
+    } else {
+        double zi = 1.0 / z, r[17];
+        r[0] = sin(z) * zi;
+        r[1] = (sin(z) - z * cos(z)) * zi * zi;
+        for (int m = 2; m <= 16; ++m) r[m] = (2 * m - 1) * r[m - 1] * zi - r[m - 2];
+        double zm = 1.0;
+        for (int m = 0; m <= lmax; ++m) { j[m] = r[m] * zm; zm *= zi; }
+    }
+    for (int m = 0; m <= lmax; ++m)
+        if (fabs(j[m]) < 1e-16) j[m] = 0.0;
+}
+
 /* Contracted Cartesian block (ab|cd), unnormalised components, row-major
  * [ncart(la)][ncart(lb)][ncart(lc)][ncart(ld)]. */
 static void eri_cart(const or_shell *sa, const or_shell *sb, const or_shell *sc, const or_shell *sd, double *out)
@@ -345,11 +400,33 @@ static void eri_cart(const or_shell *sa, const or_shell *sb, const or_shell *sc,
                 PQ2 += (P[i] - Q[i]) * (P[i] - Q[i]);
             }
             double F[OR_MAXLT + 1];
-            oracle_boys(L, rho * PQ2, F);
-            /* [00|00]^(m) = 2 pi^{5/2}/(zeta eta sqrt(zeta+eta)) K_AB K_CD F_m
-             *             = sqrt(2/pi) U_P U_Q sqrt(2 rho) F_m   (two_electron_fundamentals.c:71 at m=0) */
-            double pre = sqrt(2.0 / M_PI) * UP * UQ * sqrt(2.0 * rho);
-            for (int m = 0; m <= L; ++m) V[0][0][m] = pre * F[m];
+            if (g_op == 0) {
+                oracle_boys(L, rho * PQ2, F);
+                /* [00|00]^(m) = 2 pi^{5/2}/(zeta eta sqrt(zeta+eta)) K_AB K_CD F_m
+                 *             = sqrt(2/pi) U_P U_Q sqrt(2 rho) F_m   (two_electron_fundamentals.c:71 at m=0) */
+                double pre = sqrt(2.0 / M_PI) * UP * UQ * sqrt(2.0 * rho);
+                for (int m = 0; m <= L; ++m) V[0][0][m] = pre * F[m];
+            } else {
+                /* j0(S r12): (-d/dT)^m of U_P U_Q exp(-S^2/(4 rho)) j0(S R), T = rho R^2 */
+                double S = g_S, U = UP * UQ;
+                if (S < 1e-14) {
+                    V[0][0][0] = U;
+                    for (int m = 1; m <= L; ++m) V[0][0][m] = 0.0;
+                } else {
+                    double eS = exp(-0.25 * S * S / rho), step = S * S / (2.0 * rho), sp = 1.0;
+                    if (PQ2 < 1e-14) {
+                        double df = 1.0;
+                        for (int m = 0; m <= L; ++m) {
+                            df *= (double)(2 * m + 1);
+                            V[0][0][m] = U * eS * sp / df;
+                            sp *= step;
+                        }
+                    } else {
+                        oracle_sph_bessel(L, S * sqrt(PQ2), F);
+                        for (int m = 0; m <= L; ++m) { V[0][0][m] = U * eS * sp * F[m]; sp *= step; }
+                    }
+                }
+            }
             double o2z = 0.5 / zeta, o2e = 0.5 / eta, o2ze = 0.5 / (zeta + eta);
             double rz = rho / zeta, re = rho / eta;
             /* bra VRR */

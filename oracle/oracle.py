@@ -70,6 +70,8 @@ def lib():
         L.oracle_eri_list.argtypes = [P(OrShell), ctypes.c_int, P(ctypes.c_int)]
         L.oracle_eri_list.restype = ctypes.c_double
         L.oracle_boys.argtypes = [ctypes.c_int, ctypes.c_double, P(ctypes.c_double)]
+        L.oracle_set_operator.argtypes = [ctypes.c_int, ctypes.c_double]
+        L.oracle_sph_bessel.argtypes = [ctypes.c_int, ctypes.c_double, P(ctypes.c_double)]
         assert L.oracle_sizeof_shell() == ctypes.sizeof(OrShell)
         _lib = L
     return _lib
@@ -185,7 +187,16 @@ class Basis:
                     out.append((a, b, c, d))
         return out
 
-    def eri_dense(self):
+    def eri_dense(self, scattering=None):
+        """Dense ERI tensor over the screened quartets (hartree_fock.py:241-327); with
+        scattering = S the operator is j0(S r12) (the integrals of
+        Methods/properties.py:20-23), screened by its own Schwarz bounds."""
+        if scattering is not None:
+            lib().oracle_set_operator(1, float(scattering))
+            try:
+                return self.eri_dense()
+            finally:
+                lib().oracle_set_operator(0, 0.0)
         n = self.nbf
         eri = np.zeros((n, n, n, n))
         for (a, b, c, d) in self.quartets():
@@ -615,3 +626,24 @@ def noci_assemble(occupancy, C, hf_occupancy):
         else:
             raise ValueError("spin-flip determinant needs an orbital its Hartree-Fock state leaves empty")
     return out
+
+
+# ------------------------------------------------------------------------------------
+# Electron scattering (Methods/properties.py)
+# ------------------------------------------------------------------------------------
+def sph_bessel_scaled(lmax, z):
+    """z^-m j_m(z), m = 0..lmax, by the piecewise scheme of spherical_bessel_j.c."""
+    out = np.zeros(lmax + 1)
+    lib().oracle_sph_bessel(lmax, float(z), _dp(out))
+    return out
+
+
+def scattering_intensity(Da, Db, eri_S, n_electrons):
+    """Total scattering intensity of one state at one momentum transfer,
+    Methods/properties.py:20-23,41-73: N + sum_abcd [P_ab P_cd - (Pa_ad Pa_cb +
+    Pb_ad Pb_cb)] (ab|j0(S r12)|cd)."""
+    P = Da + Db
+    v = np.einsum("ab,cd,abcd->", P, P, eri_S, optimize=True)
+    v -= np.einsum("ad,cb,abcd->", Da, Da, eri_S, optimize=True)
+    v -= np.einsum("ad,cb,abcd->", Db, Db, eri_S, optimize=True)
+    return n_electrons + float(v)

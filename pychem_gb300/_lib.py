@@ -72,6 +72,8 @@ _SIGS = {
                          c_void_p, c_void_p, c_void_p],
     "pcg_digest_class_u": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "pcg_scattering_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int,
+                             ctypes.c_double, c_void_p, c_void_p],
     "pcg_digest_class_co": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p, c_int,
                             c_void_p, c_void_p, c_void_p, c_void_p],
     "pcg_fock_build": [c_int, c_void_p, c_void_p, c_void_p, c_void_p],
@@ -96,7 +98,7 @@ _SIGS = {
 }
 # entry points that launch exactly one kernel of this library per call
 LAUNCHERS = {"pcg_pair_data", "pcg_pair_data_f32", "pcg_pair_ao", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
-             "pcg_digest_class", "pcg_digest_class_u", "pcg_digest_class_co", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh", "pcg_mlp_gemm", "pcg_mlp_dsilu",
+             "pcg_digest_class", "pcg_digest_class_u", "pcg_digest_class_co", "pcg_scattering_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh", "pcg_mlp_gemm", "pcg_mlp_dsilu",
              "pcg_mlp_colsum", "pcg_mlp_mse", "pcg_mlp_adam",
              "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",
              "pcg_two_electron_vrr", "pcg_two_electron_contract", "pcg_two_electron_hrr",

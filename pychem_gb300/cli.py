@@ -11,10 +11,13 @@ calculation runs in the last one; the upstream basis-fitting bootstrap through t
 earlier ones only supplies starting orbitals), ``Coords``, ``Coords_Units`` (ANGSTROM,
 BOHR), ``Charge``, ``Multiplicity``, ``Max_SCF_Iterations``, ``Excitations`` (HOMO-LUMO:
 the alpha HOMO -> LUMO state by MOM after the ground state, as ``pychem.py:64-86``),
-``Constrain_Excited``, ``Job_Type`` / ``Property_Type``.  ``Method = "NOCI"`` runs the
-states of any ``Excitations`` keyword (spin-flip lists included) and the NOCI of
-``Methods/noci.py`` (pychem_gb300.noci).  Scattering properties are not part of this
-build: such sections run their Hartree-Fock part and report the rest as unavailable.
+``Constrain_Excited``, ``Job_Type`` / ``Property_Type`` / ``Property_Grid``.
+``Method = "NOCI"`` runs the states of any ``Excitations`` keyword (spin-flip lists
+included) and the NOCI of ``Methods/noci.py`` (pychem_gb300.noci).
+``Job_Type = "PROPERTY"`` with ``Property_Type = "SCATTERING"`` adds the total
+electron-scattering intensity of every state at every grid value
+(``Methods/properties.py:6-37``, pychem_gb300.scattering), after NOCI of its
+determinants as upstream.
 """
 import ast
 import configparser
@@ -23,7 +26,7 @@ import sys
 
 import torch
 
-from . import noci
+from . import noci, scattering
 from .engine import GpuEngine
 from .molecule import Molecule
 from .scf import rhf, rmp2, uhf, ump2
@@ -77,8 +80,9 @@ def run_section(name, opts, write):
         res["noci_energies"] = e
         write("NOCI determinants: %d" % len(out["dets_alpha"]))
         write("NOCI energies: " + " ".join("%.11f" % x for x in e))
-        if opts.get("JOB_TYPE") == "PROPERTY":
-            write("Property %s: not available in this build" % opts.get("PROPERTY_TYPE"))
+        na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+        dens = [(a[:, :na] @ a[:, :na].T, b[:, :nb] @ b[:, :nb].T) for a, b in zip(out["dets_alpha"], out["dets_beta"])]
+        _properties(mol, opts, dens, res, write)
         return res
     if ref == "RHF":
         if mol.NAlphaElectrons != mol.NBetaElectrons:
@@ -106,9 +110,25 @@ def run_section(name, opts, write):
             entry["E_mp2_corr"] = e2
             write("State %s: MP2 correlation energy: %.11f  Total MP2 energy: %.11f" % (label, e2, st.E + e2))
         res["states"].append(entry)
-    if opts.get("JOB_TYPE") == "PROPERTY":
-        write("Property %s: not available in this build" % opts.get("PROPERTY_TYPE"))
+    _properties(mol, opts, [scattering.state_densities(st) for _, st in states], res, write)
     return res
+
+
+def _properties(mol, opts, densities, res, write):
+    """Job_Type = PROPERTY (Methods/properties.py:6-37): the scattering table, grid value
+    then one intensity per state, as upstream prints it."""
+    if opts.get("JOB_TYPE") != "PROPERTY":
+        return
+    kind = opts.get("PROPERTY_TYPE")
+    if kind != "SCATTERING":
+        write("Property %s: not available in this build" % kind)
+        return
+    grid = [float(x) for x in opts["PROPERTY_GRID"]]
+    table = scattering.intensities(mol, grid, densities)
+    res["scattering"] = {"grid": grid, "intensities": table.tolist()}
+    write("Grid value -> Scattering patterns for each electronic state")
+    for S, row in zip(grid, table):
+        write("%10.6f" % S + "".join("%16.12f" % v for v in row))
 
 
 def run_file(path, stream=sys.stdout):

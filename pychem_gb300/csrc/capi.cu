@@ -133,6 +133,15 @@ int pcg_digest_class_u(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pai
                              GKb, (cudaStream_t)stream);
 }
 
+int pcg_scattering_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                         double S, double* store, void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs || ntask < 0 || !(S >= 0.0)) {
+    pcg_set_error("pcg_scattering_class: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  return pcg_launch_scattering(cls, to_dev(pairs), (const int2*)tasks, ntask, S, store, (cudaStream_t)stream);
+}
+
 int pcg_digest_class_co(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
                         const double* store, int nd, const double* W, double* GJ, double* GK, void* stream) {
   if (cls < 0 || cls > 20 || !basis || !pairs || nd < 0 || (nd > 0 && (!W || !GJ || !GK))) {

@@ -204,6 +204,16 @@ int pcg_launch_eri(int cls, const DevBasis& b, const DevPairsExt& pr, const Boys
   return pcg_launch_eri_g5(cls, pr, bt, tasks, ntask, store, precision, s);
 }
 
+int pcg_launch_scattering(int cls, const DevPairsExt& pr, const int2* tasks, int ntask, double S, double* store,
+                          cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  if (cls < 0 || cls > 20) return PCG_ERR_ARG;
+  if (cls <= 13) return pcg_launch_eri_s0(cls, pr, tasks, ntask, S, store, s);
+  if (cls <= 17) return pcg_launch_eri_s1(cls, pr, tasks, ntask, S, store, s);
+  if (cls <= 19) return pcg_launch_eri_s2(cls, pr, tasks, ntask, S, store, s);
+  return pcg_launch_eri_s3(cls, pr, tasks, ntask, S, store, s);
+}
+
 int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                       const double* store, const double* D, double* G, cudaStream_t s) {
   if (ntask <= 0) return PCG_OK;

@@ -36,6 +36,16 @@ int pcg_launch_eri(int cls, const DevBasis& b, const DevPairsExt& pr, const Boys
 int pcg_launch_pair_data_f32(int npp, const double* zeta, const double* PA, const double* oo2z, const float* Kf,
                              float* pf8, cudaStream_t s);
 int pcg_launch_pair_ao(const DevBasis& b, int npair, const int* pA, const int* pB, int* ao4, cudaStream_t s);
+int pcg_launch_eri_s0(int cls, const DevPairsExt& pr, const int2* tasks, int ntask, double S, double* store,
+                      cudaStream_t s);
+int pcg_launch_eri_s1(int cls, const DevPairsExt& pr, const int2* tasks, int ntask, double S, double* store,
+                      cudaStream_t s);
+int pcg_launch_eri_s2(int cls, const DevPairsExt& pr, const int2* tasks, int ntask, double S, double* store,
+                      cudaStream_t s);
+int pcg_launch_eri_s3(int cls, const DevPairsExt& pr, const int2* tasks, int ntask, double S, double* store,
+                      cudaStream_t s);
+int pcg_launch_scattering(int cls, const DevPairsExt& pr, const int2* tasks, int ntask, double S, double* store,
+                          cudaStream_t s);
 int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                       const double* store, const double* D, double* G, cudaStream_t s);
 int pcg_launch_digest_u(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,

@@ -248,7 +248,17 @@ class GpuEngine:
         self.S, self.H = S, H
         return S, H
 
+    # two-electron operator: None for 1/r12, S >= 0 for j0(S r12) (electron scattering,
+    # Methods/properties.py:20-23); schwarz(), build_tasks() and compute_eris() follow it
+    scattering = None
+
     def _eri(self, cls, tasks, ntask, store, fp32):
+        if self.scattering is not None:
+            if fp32:
+                raise ValueError("scattering integrals are FP64 only")
+            _lib.call("pcg_scattering_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
+                      _ptr(tasks), ntask, float(self.scattering), _ptr(store), _stream())
+            return
         _lib.call("pcg_eri_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t), _ptr(tasks), ntask,
                   _ptr(store), 1 if fp32 else 0, _stream())
 
