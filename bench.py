@@ -410,6 +410,69 @@ def noci_leg(torch, args):
             "ci_speedup_vs_cpu_oracle": cpu_per_pair * npairs / t_ci}
 
 
+def _cpu_scat_worker(args):
+    """Time the C oracle on a list of j0(S r12) quartets (one process, operator set)."""
+    atoms, basis, S, quads = args
+    import ctypes
+    import numpy as np
+    from oracle import oracle as O
+    b = O.Basis(atoms, basis)
+    O.lib().oracle_set_operator(1, float(S))
+    q = np.ascontiguousarray(np.asarray(quads, dtype=np.int32).reshape(-1))
+    t0 = time.perf_counter()
+    O.lib().oracle_eri_list(b.c, len(quads), q.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    t = time.perf_counter() - t0
+    O.lib().oracle_set_operator(0, 0.0)
+    return t
+
+
+def scattering_leg(torch, args):
+    """Total electron-scattering intensities (Methods/properties.py) of the RHF ground
+    state of (H2O)8 / 6-31G on a 16-point grid S = 0 .. 7.5 bohr^-1: per grid value the
+    j0(S r12) Schwarz pass, quartet plan, integral store and contraction with the
+    state's densities.  CPU: the C oracle's j0(S r12) quartets/s on a bounded sample
+    at S = 2, times the quartets its screen keeps there (contraction not added)."""
+    import numpy as np
+    from pychem_gb300 import scattering, workloads as W
+    from pychem_gb300.engine import GpuEngine
+    from pychem_gb300.molecule import Molecule
+    from pychem_gb300.scf import rhf
+    from oracle import oracle as O
+    mol = Molecule(W.water_cluster(2, 2, 2, seed=SEED), "6-31G")
+    r = rhf(GpuEngine(mol).prepare())
+    grid = [0.5 * k for k in range(16)]
+    dens = [(r.D, r.D)]
+    scattering.intensities(mol, grid[:2], dens)            # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    table = scattering.intensities(mol, grid, dens)
+    torch.cuda.synchronize()
+    t_gpu = time.perf_counter() - t0
+    # CPU sample at S = 2
+    atoms = [(a[0], a[1], *a[2]) for a in mol.atoms]
+    b = O.Basis(atoms, "6-31G")
+    S_cpu = 2.0
+    O.lib().oracle_set_operator(1, S_cpu)
+    try:
+        quads = np.array(b.quartets(), dtype=np.int32)
+    finally:
+        O.lib().oracle_set_operator(0, 0.0)
+    rng = np.random.default_rng(SEED)
+    probe = quads[rng.choice(len(quads), size=min(len(quads), 1500), replace=False)]
+    per = _cpu_scat_worker((atoms, "6-31G", S_cpu, probe)) / len(probe)
+    n = int(min(len(quads), max(1500, 10.0 / per)))
+    sample = quads[rng.choice(len(quads), size=n, replace=False)]
+    rate = n / _cpu_scat_worker((atoms, "6-31G", S_cpu, sample))
+    return {"workload": "(H2O)8 6-31G (%d AO), RHF ground state, %d grid values S = 0..%.1f" % (
+                mol.NOrbitals, len(grid), grid[-1]),
+            "gpu_s": t_gpu, "gpu_s_per_grid_value": t_gpu / len(grid),
+            "intensity_S0": float(table[0, 0]), "intensity_S2": float(table[4, 0]),
+            "cpu_quartets_per_s": rate, "cpu_quartets_S2": int(len(quads)),
+            "cpu_s_per_grid_value_S2": len(quads) / rate, "cpu_sample": "%d of %d quartets at S = 2, 1 core" % (
+                n, len(quads)),
+            "speedup_per_grid_value": (len(quads) / rate) / (t_gpu / len(grid))}
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -528,6 +591,7 @@ def gpu_arm(args):
     alk = alkane_leg(torch, args) if world == 1 or rank == 0 else None
     lrn = learned_leg(torch, args) if world == 1 or rank == 0 else None
     nci = noci_leg(torch, args) if world == 1 or rank == 0 else None
+    sct = scattering_leg(torch, args) if world == 1 or rank == 0 else None
 
     # max over ranks
     if world > 1:
@@ -579,6 +643,7 @@ def gpu_arm(args):
         "alkane_mixed": alk,
         "learned_guess": lrn,
         "noci_spin_flip": nci,
+        "scattering": sct,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": out["h2d_bytes"],
                 "d2h_bytes_per_step": out["d2h_bytes"]},
         "gpu_launches": launches,
