@@ -6,6 +6,10 @@ cases:  water16 ((H2O)16 / 6-31G, 208 AO), water8 ((H2O)8, 104 AO), water4 ((H2O
         alkane12 (C12H26 / cc-pVDZ, 298 AO), ensemble (256 perturbed small molecules,
         6-31G, batched), mlp (the learned-guess network on 65,536 pairs)
 phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2);
+        scattering (one j0(S r12) grid value at --S: Schwarz pass, quartet plan,
+        integral store, contraction with the RHF densities, each timed);
+        noci (the CI matrix of C2 / cc-pVDZ spin-flip doubles with CISD, 27
+        determinants; --case is ignored);
         for mlp: train (forward, loss, backward, Adam)
 """
 import argparse
@@ -29,7 +33,8 @@ CASES = {
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="water16", choices=sorted(CASES) + ["ensemble", "mlp"])
-    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train"])
+    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train", "scattering", "noci"])
+    ap.add_argument("--S", type=float, default=2.0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
@@ -37,7 +42,11 @@ def main():
         return ensemble_case(args)
     if args.case == "mlp":
         return mlp_case(args)
+    if args.phase == "noci":
+        return noci_case(args)
     mol = CASES[args.case]()
+    if args.phase == "scattering":
+        return scattering_case(args, mol)
     eng = GpuEngine(mol, precision=args.precision)
     eng.one_electron(); eng.schwarz(); eng.build_tasks(); eng.compute_eris()
     torch.cuda.synchronize()
@@ -95,3 +104,39 @@ def mlp_case(args):
 
 if __name__ == "__main__":
     main()
+
+
+def _timed(fn):
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def scattering_case(args, mol):
+    """One grid value of the scattering intensity, phase by phase."""
+    r = rhf(GpuEngine(mol).prepare())
+    eng = GpuEngine(mol)
+    eng.one_electron()
+    for k in range(args.repeat + 1):
+        eng.scattering = args.S
+        _, t_q = _timed(eng.schwarz)
+        _, t_p = _timed(eng.build_tasks)
+        _, t_e = _timed(eng.compute_eris)
+        (Fa, Fb), t_c = _timed(lambda: eng.fock_u(r.D, r.D))
+        if k:
+            print("%s scattering S=%.2f: schwarz %.4f s, plan %.4f s, integrals %.4f s (%d quartets), "
+                  "contraction %.4f s" % (args.case, args.S, t_q, t_p, t_e, eng.stats["quartets"], t_c))
+
+
+def noci_case(args):
+    """The CI matrix of spin-flip NOCI on C2 / cc-pVDZ (SFD-CISD)."""
+    from . import noci
+    mol = Molecule([["C", 6.0, 0.0, 0.0, 0.0], ["C", 6.0, 1.25, 0.0, 0.0]], "cc-pVDZ")
+    eng = GpuEngine(mol).prepare()
+    out = noci.run(eng, "SFD-CISD", reference="UHF", constrain_excited=True)
+    na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+    for _ in range(args.repeat + 1):
+        _, t = _timed(lambda: noci.noci_matrix(eng, out["dets_alpha"], out["dets_beta"], na, nb))
+    print("noci C2 cc-pVDZ SFD-CISD: %d determinants, CI matrix %.4f s" % (len(out["dets_alpha"]), t))
