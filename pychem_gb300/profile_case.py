@@ -102,9 +102,6 @@ def mlp_case(args):
     print("mlp train step: %.4f s per repeat" % ((time.perf_counter() - t0) / args.repeat))
 
 
-if __name__ == "__main__":
-    main()
-
 
 def _timed(fn):
     torch.cuda.synchronize()
@@ -140,3 +137,7 @@ def noci_case(args):
     for _ in range(args.repeat + 1):
         _, t = _timed(lambda: noci.noci_matrix(eng, out["dets_alpha"], out["dets_beta"], na, nb))
     print("noci C2 cc-pVDZ SFD-CISD: %d determinants, CI matrix %.4f s" % (len(out["dets_alpha"]), t))
+
+
+if __name__ == "__main__":
+    main()
