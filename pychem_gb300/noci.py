@@ -326,13 +326,75 @@ def determinants(states, results, spin_flip_list):
 # ------------------------------------------------------------------------------------
 # CI matrix (Methods/noci.py:51-109)
 # ------------------------------------------------------------------------------------
+DEGENERATE = 1.0e-8           # singular values closer than this form one cluster
+
+
+def _canonical(U, V, s):
+    """Fix the singular vectors inside each cluster of equal singular values.
+
+    An SVD determines them only up to a rotation inside such a cluster (and, for the
+    zero cluster, independent rotations of U and V), while upstream's two-zero element
+    (noci.py:279-300) reads single pairs out of it, so its value follows the solver's
+    arbitrary choice and jumps under rounding-level changes of the orbitals.  Here each
+    cluster's columns become the eigenvectors of U_c^T diag(1..n) U_c (V_c^T diag(1..n)
+    V_c for the zero cluster's V), ordered by eigenvalue: a choice that depends only on
+    the subspaces and varies continuously with them.  Elements that do not depend on
+    the basis (all others) are unchanged; signs are left to the phase rule."""
+    P, n = s.shape
+    if n < 2:
+        return U, V
+    dev, dt = s.device, s.dtype
+    zero = s <= NOCI_THRESH
+    split = ((s[:, :-1] - s[:, 1:]) > DEGENERATE) | (zero[:, :-1] != zero[:, 1:])
+    brk = torch.cat([torch.ones(P, 1, dtype=torch.bool, device=dev), split & ~(zero[:, :-1] & zero[:, 1:])], dim=1)
+    label = torch.cumsum(brk.to(torch.int64), dim=1)                      # 1, 2, ... per cluster
+    same = label.unsqueeze(2) == label.unsqueeze(1)
+    Dg = torch.arange(1, n + 1, dtype=dt, device=dev)
+    shift = torch.diag_embed(label.to(dt) * (4.0 * n))                    # keeps blocks apart
+
+    def rotation(X, blocks):
+        K = (X.transpose(1, 2) * Dg) @ X
+        K = 0.5 * (K + K.transpose(1, 2))
+        _, Q = torch.linalg.eigh(torch.where(blocks, K, torch.zeros((), dtype=dt, device=dev)) + shift)
+        return Q
+
+    Qu = rotation(U, same)
+    # V follows U's rotation except in the zero cluster, whose V columns get their own
+    # (both matrices are block diagonal over the same clusters)
+    Qv = torch.where(zero.unsqueeze(1), rotation(V, same), Qu)
+    return U @ Qu, V @ Qv
+
+
+def _first_large_sign(X):
+    """Per column: the sign of its first entry with at least half the largest
+    magnitude (a sign choice that small changes of X do not flip)."""
+    mag = X.abs()
+    big = mag >= 0.5 * mag.amax(dim=1, keepdim=True)
+    k = big.to(torch.int8).argmax(dim=1, keepdim=True)
+    return torch.where(X.gather(1, k) < 0, -1.0, 1.0).to(X.dtype)
+
+
 def _pair(C1, C2, S, n):
-    """Batched Lowdin pairing (noci.py:183-205): C1, C2 (P, nbf, >= n)."""
+    """Batched Lowdin pairing (noci.py:183-205): C1, C2 (P, nbf, >= n); singular
+    vectors canonical inside degenerate clusters (_canonical).
+
+    Phases as upstream: the second orbital of a pair flips when the plain dot product
+    of the two is negative.  Where that dot product vanishes (orbitals of different
+    symmetry on disjoint functions) upstream's choice is rounding noise; there the pair
+    keeps a positive overlap if it has one, and a zero-overlap pair fixes each orbital's
+    sign by its first large coefficient."""
     A, B = C1[:, :, :n], C2[:, :, :n]
-    U, _, Vh = torch.linalg.svd(A.transpose(1, 2) @ S @ B)
-    A2, B2 = A @ U, B @ Vh.transpose(1, 2)
-    sign = torch.where((A2 * B2).sum(dim=1) < 0, -1.0, 1.0).to(B2.dtype)
-    return A2, B2 * sign.unsqueeze(1)
+    U, s, Vh = torch.linalg.svd(A.transpose(1, 2) @ S @ B)
+    U, V = _canonical(U, Vh.transpose(1, 2), s)
+    A2, B2 = A @ U, B @ V
+    dot = (A2 * B2).sum(dim=1)
+    ov = ((A2.transpose(1, 2) @ S) * B2.transpose(1, 2)).sum(dim=2)
+    tiny = dot.abs() <= 1e-10 * A2.norm(dim=1) * B2.norm(dim=1)
+    zero = tiny & (ov.abs() <= NOCI_THRESH)
+    A2 = torch.where(zero.unsqueeze(1), A2 * _first_large_sign(A2), A2)
+    B2 = torch.where(zero.unsqueeze(1), B2 * _first_large_sign(B2), B2)
+    flip = torch.where(tiny, ~zero & (ov < 0), dot < 0)
+    return A2, torch.where(flip.unsqueeze(1), -B2, B2)
 
 
 def noci_matrix(engine, dets_a, dets_b, na, nb, return_pairs=False):
