@@ -9,7 +9,10 @@ The reference's NOCI (``Methods/noci.py``) runs after the Hartree-Fock states th
 
 * Lowdin pairing of each pair's occupied orbitals by a batched SVD of C1_o^T S C2_o, the
   second orbital of a pair sign-flipped when its plain dot product with the first is
-  negative (``noci.py:183-205``);
+  negative (``noci.py:183-205``); where upstream leaves the pairing to the solver
+  (degenerate singular values) or the phase to rounding (a vanishing dot product),
+  canonical choices make the CI matrix a continuous function of the orbitals
+  (_canonical, _pair);
 * paired overlaps, the reduced overlap over those above 1e-8 and the zero list
   (``noci.py:215-223``); co-densities W = sum_i c1_i c2_i^T / s_i, or the pair densities
   P of a zero (``noci.py:207-213,261-300``);
