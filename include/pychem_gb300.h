@@ -56,10 +56,11 @@ int pcg_shellpair_quantities(double *sigmas, double *overlaps, double *centres,
 int pcg_two_electron_bound(double *bounds, const double *C_P, const double *C_Q,
                            int nla, int nlb, int nlc, int nld);
 
-/* Methods/_c_ints.c:195-245 (c_ints/two_electron_fundamentals.c:6-95).
+/* Methods/_c_ints.c:195-245 (c_ints/two_electron_fundamentals.c:6-95; with
+ * ints_type 1 c_ints/two_electron_scattering.c:6-81, the j0(S r12) operator at
+ * S = grid_value >= 0, z^-m j_m(z) by the regimes of spherical_bessel_j.c).
  * fundamentals [m+1][na*nb][nc*nd]; sigma/U [na][nb], [nc][nd]; P [na][nb][3];
- * Q [nc][nd][3]; R [na*nb][nc*nd][3] (output).  ints_type 1 (scattering) is not
- * part of this library and returns PCG_ERR_UNSUPPORTED. */
+ * Q [nc][nd][3]; R [na*nb][nc*nd][3] (output). */
 int pcg_two_electron_fundamentals(double *fundamentals, const double *sigma_P, const double *U_P,
                                   const double *P, const double *sigma_Q, const double *U_Q,
                                   const double *Q, double *R, int na, int nb, int nc, int nd,

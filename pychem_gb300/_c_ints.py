@@ -8,9 +8,10 @@ libpychem_gb300.so on the GPU (include/pychem_gb300.h, section 1).
 Error behaviour: a wrong argument type raises ``TypeError("Error parsing objects
 passed to C")`` as upstream; arrays too small for the requested shapes raise
 ValueError (upstream reads out of bounds); output arrays must be C-contiguous and
-writeable (upstream silently writes into a temporary copy otherwise).  Scattering
-fundamentals (``ints_type == 1``) are not part of this library and raise
-NotImplementedError.
+writeable (upstream silently writes into a temporary copy otherwise).
+``two_electron_fundamentals`` with ``ints_type == 1`` gives the j0(S r12) scattering
+fundamentals at S = ``grid_value`` (``two_electron_scattering.c``), any other type the
+1/r12 ones, as upstream branches.
 
 Usage from the upstream tree: put this package on sys.path and ``import
 pychem_gb300._c_ints as _c_ints`` in place of the compiled extension.
@@ -80,8 +81,6 @@ def two_electron_bound(bounds, C_P, C_Q, nla, nlb, nlc, nld):
 def two_electron_fundamentals(fundamentals, sigma_P, U_P, P, sigma_Q, U_Q, Q, R, na, nb, nc, nd, m, ints_type,
                               grid_value):
     na, nb, nc, nd, m, ints_type = _int(na, nb, nc, nd, m, ints_type)
-    if ints_type != 0:
-        raise NotImplementedError("scattering fundamentals (ints_type 1) are not part of pychem_gb300")
     nbra, nket = na * nb, nc * nd
     f, r = _out(fundamentals, (m + 1) * nbra * nket), _out(R, 3 * nbra * nket)
     sp, up, pp = _in(sigma_P, nbra), _in(U_P, nbra), _in(P, 3 * nbra)

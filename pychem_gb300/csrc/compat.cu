@@ -13,6 +13,7 @@
 #include "../../include/pychem_gb300.h"
 #include "common.cuh"
 #include "pcg_internal.h"
+#include "scat_fund.cuh"
 
 namespace {
 
@@ -106,6 +107,39 @@ __global__ void k_fund2(BoysTable bt, double* fund, const double* sP, const doub
       boys_eval_rt(bt, lmax, th2 * r2, F);
     }
     for (int m = 0; m <= lmax; ++m) fund[(size_t)m * nbra * nket + t] = pf * U * pow(2.0 * th2, m + 0.5) * F[m];
+  }
+}
+
+// j0(S r12) fundamentals in the reference's form (two_electron_scattering.c:6-81):
+// U_P U_Q exp(-S^2 (sigma_P + sigma_Q)/4) S^2m z^-m j_m(z), z = S |P - Q|, with its S = 0
+// case (U at m = 0, zero above) and R = 0 case (z^-m j_m -> 1/(2m+1)!!).
+__global__ void k_fund_scat(double* fund, const double* sP, const double* UP, const double* P, const double* sQ,
+                            const double* UQ, const double* Q, double* R, int nbra, int nket, int lmax, double S) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nbra * nket; t += gridDim.x * blockDim.x) {
+    const int ib = t / nket, ik = t % nket;
+    const double U = UP[ib] * UQ[ik];
+    double r2 = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      const double r = P[3 * ib + i] - Q[3 * ik + i];
+      R[3 * t + i] = r;
+      r2 += r * r;
+    }
+    double F[PCG_MAXLT + 1];
+    if (S < 1e-14) {
+      F[0] = U;
+      for (int m = 1; m <= lmax; ++m) F[m] = 0.0;
+    } else {
+      const double eS = exp(-0.25 * S * S * (sP[ib] + sQ[ik]));
+      if (r2 < 1e-14) {
+        double df = 1.0;
+        for (int m = 0; m <= lmax; ++m) { df *= (double)(2 * m + 1); F[m] = 1.0 / df; }
+      } else {
+        sph_bessel_scaled_rt(lmax, S * sqrt(r2), F);
+      }
+      double sp = U * eS;
+      for (int m = 0; m <= lmax; ++m) { F[m] *= sp; sp *= S * S; }
+    }
+    for (int m = 0; m <= lmax; ++m) fund[(size_t)m * nbra * nket + t] = F[m];
   }
 }
 
@@ -326,23 +360,29 @@ int pcg_two_electron_bound(double* bounds, const double* C_P, const double* C_Q,
 int pcg_two_electron_fundamentals(double* fundamentals, const double* sigma_P, const double* U_P, const double* P,
                                   const double* sigma_Q, const double* U_Q, const double* Q, double* R, int na,
                                   int nb, int nc, int nd, int m, int ints_type, double grid_value) {
-  (void)grid_value;
-  if (ints_type != 0) {
-    pcg_set_error("two_electron_fundamentals: scattering integrals (ints_type 1) are not part of this library");
-    return PCG_ERR_UNSUPPORTED;
-  }
   ARGCHK(na > 0 && nb > 0 && nc > 0 && nd > 0 && m >= 0, "two_electron_fundamentals: bad arguments");
   if (m > PCG_MAXLT) { pcg_set_error("two_electron_fundamentals: Boys order above 8 (shells above d)"); return PCG_ERR_UNSUPPORTED; }
+  // ints_type 1: j0(S r12) scattering operator at S = grid_value; anything else: 1/r12
+  // (the reference's branch, _c_ints.c:236-240)
+  if (ints_type == 1 && !(grid_value >= 0.0)) {
+    pcg_set_error("two_electron_fundamentals: scattering needs grid_value >= 0");
+    return PCG_ERR_ARG;
+  }
   BoysTable bt;
-  if (int rc = pcg_ensure_boys(&bt)) return rc;
+  if (ints_type != 1)
+    if (int rc = pcg_ensure_boys(&bt)) return rc;
   const size_t nbra = (size_t)na * nb, nket = (size_t)nc * nd;
   Arena ar;
   int f = ar.add(nullptr, (m + 1) * nbra * nket), r = ar.add(nullptr, 3 * nbra * nket);
   int sp = ar.add(sigma_P, nbra), up = ar.add(U_P, nbra), pp = ar.add(P, 3 * nbra);
   int sq = ar.add(sigma_Q, nket), uq = ar.add(U_Q, nket), qq = ar.add(Q, 3 * nket);
   if (int rc = ar.stage()) return rc;
-  k_fund2<<<grid(nbra * nket), 128>>>(bt, ar.d(f), ar.d(sp), ar.d(up), ar.d(pp), ar.d(sq), ar.d(uq), ar.d(qq),
-                                      ar.d(r), (int)nbra, (int)nket, m);
+  if (ints_type == 1)
+    k_fund_scat<<<grid(nbra * nket), 128>>>(ar.d(f), ar.d(sp), ar.d(up), ar.d(pp), ar.d(sq), ar.d(uq), ar.d(qq),
+                                            ar.d(r), (int)nbra, (int)nket, m, grid_value);
+  else
+    k_fund2<<<grid(nbra * nket), 128>>>(bt, ar.d(f), ar.d(sp), ar.d(up), ar.d(pp), ar.d(sq), ar.d(uq), ar.d(qq),
+                                        ar.d(r), (int)nbra, (int)nket, m);
   LAUNCH_DONE();
   if (int rc = ar.fetch(f, fundamentals)) return rc;
   return ar.fetch(r, R);

@@ -8,6 +8,7 @@ its own output table, which differs where its Schwarz screen drops quartets (tho
 the previous pass's values in the reference's integral tensor).
 """
 import glob
+import math
 import os
 
 import numpy as np
@@ -97,3 +98,49 @@ def test_zero_momentum_transfer_gives_n_squared():
     z = load("scat_lih_uhf_631g")
     n = int(z["n_electrons"])
     assert abs(z["clean"][0][0] - n * n) < 1e-9
+
+
+def _reference_form_fundamentals(sP, UP, P, sQ, UQ, Q, lmax, S):
+    """two_electron_scattering.c:6-81 restated with the oracle's Bessel scheme:
+    U_P U_Q exp(-S^2 (sigma_P + sigma_Q)/4) S^2m z^-m j_m(z), z = S |P - Q|."""
+    nbra, nket = sP.size, sQ.size
+    out = np.zeros((lmax + 1, nbra, nket))
+    Pf, Qf = P.reshape(nbra, 3), Q.reshape(nket, 3)
+    for i in range(nbra):
+        for k in range(nket):
+            U = UP.flat[i] * UQ.flat[k]
+            r2 = float(np.sum((Pf[i] - Qf[k]) ** 2))
+            if S < 1e-14:
+                out[0, i, k] = U
+                continue
+            eS = math.exp(-0.25 * S * S * (sP.flat[i] + sQ.flat[k]))
+            s2 = np.array([S ** (2 * m) for m in range(lmax + 1)])
+            if r2 < 1e-14:
+                j = np.array([1.0 / np.prod(np.arange(1, 2 * m + 2, 2)) for m in range(lmax + 1)])
+            else:
+                j = oracle.sph_bessel_scaled(lmax, S * math.sqrt(r2))
+            out[:, i, k] = U * eS * s2 * j
+    return out
+
+
+def test_recorded_scattering_fundamentals():
+    """The reference's compiled j0(S r12) fundamentals (recorded by
+    make_golden_c_ints_scattering.py) against the restatement, every regime."""
+    import json
+    with open(os.path.join(HERE, "golden", "c_ints_scattering_calls.json")) as fh:
+        manifest = json.load(fh)
+    arrays = np.load(os.path.join(HERE, "golden", "c_ints_scattering_calls.npz"))
+    n = 0
+    for call in manifest:
+        if call["fn"] != "two_electron_fundamentals":
+            continue
+        a = call["args"]
+        get = lambda k: arrays[a[k][1]]
+        lmax, itype, S = int(a[12][1]), int(a[13][1]), float(a[14][1])
+        assert itype == 1
+        want = arrays[[o for i, o in call["outputs"] if i == 0][0]]
+        got = _reference_form_fundamentals(get(1), get(2), get(3), get(4), get(5), get(6), lmax, S)
+        scale = max(1.0, float(np.abs(want).max()))
+        assert np.abs(got.reshape(want.shape) - want).max() <= 1e-13 * scale, S
+        n += 1
+    assert n == 24
