@@ -23,6 +23,14 @@ import this module, always as the checker.  It restates the upstream algorithm:
   DIIS of ``Methods/hf_extensions/diis.py`` and the CUHF constraint of
   ``hartree_fock.py:359-391`` (natural orbitals of S^1/2 (D_tot/2) S^1/2), and UMP2 as
   ``Methods/mp2.py:43-101``; pinned by ``tests/test_oracle_open_shell.py``.
+* NOCI: the CI matrix of ``Methods/noci.py:51-318`` (Lowdin pairing by numpy's SVD and
+  the plain-dot-product phase rule as upstream, the no-, one- and two-zero element
+  forms, the generalised eigenproblem) and the spin-flip orbital assembly of
+  ``noci.py:127-146``; pinned by ``tests/test_noci_host.py``.
+* Electron scattering: j0(S r12) integrals through ``hgp_oracle.c`` with the
+  fundamentals of ``Methods/c_ints/two_electron_scattering.c`` and the Bessel scheme of
+  ``spherical_bessel_j.c``, and the intensity contraction of
+  ``Methods/properties.py:41-73``; pinned by ``tests/test_scattering_host.py``.
 """
 import ctypes
 import json
