@@ -151,14 +151,18 @@ def excited_states(na, nb, norb, excitations=None, n_core=0, alpha_excitations=N
     Returns (states, spin_flip): states is a list of (alpha, beta) occupancy lists,
     ground state first; spin_flip a list of [state index, alpha, beta] (empty unless a
     spin-flip type).  ``excitations`` takes the upstream keywords and aliases
-    (Util/structures.py:393-413); CUSTOM-SINGLE / CUSTOM-PAIRED come from
-    alpha_excitations / beta_excitations lists of [from, to] pairs."""
+    (Util/structures.py:393-413).  Custom lists (alpha_excitations /
+    beta_excitations, upstream's CUSTOM-SINGLE and CUSTOM-PAIRED) pass upstream's
+    input check, but set_excitations has no branch for them and stops
+    (structures.py:614-618); they raise ValueError here."""
     exc = excitations.upper() if isinstance(excitations, str) else excitations
     exc = EXCITATION_ALIASES.get(exc, exc)
     if exc is None and (alpha_excitations or beta_excitations):
         exc = "CUSTOM-PAIRED" if (alpha_excitations and beta_excitations) else "CUSTOM-SINGLE"
     if exc not in EXCITATION_TYPES:
         raise ValueError("excitation type %r not recognised" % (excitations,))
+    if exc is not None and exc.startswith("CUSTOM"):
+        raise ValueError("excitation type %s not recognised in set_excitations" % exc)
     alpha_g = [1] * na + [0] * (norb - na)
     beta_g = [1] * nb + [0] * (norb - nb)
     states = [(list(alpha_g), list(beta_g))]
@@ -173,9 +177,6 @@ def excited_states(na, nb, norb, excitations=None, n_core=0, alpha_excitations=N
     elif exc in ("S", "D", "SD"):
         a_ex, b_ex = _singles(n_core, na, na, norb), _singles(n_core, nb, nb, norb)
         a_dbl, b_dbl = _doubles(n_core, na, na, norb), _doubles(n_core, nb, nb, norb)
-    elif exc.startswith("CUSTOM"):
-        a_ex = alpha_excitations or [[]]
-        b_ex = beta_excitations or [[]]
     if "SF" in exc:
         spin_flip = [[0, list(alpha_g), list(beta_g)]]
         ao, bo = list(alpha_g), list(beta_g)
@@ -204,13 +205,8 @@ def excited_states(na, nb, norb, excitations=None, n_core=0, alpha_excitations=N
                 spin_flip += _spinflip_states(alpha_g, beta_g, na, nb, 2, 1)
         return states, [[s[0], list(s[1]), list(s[2])] for s in spin_flip]
     beta_o = beta_g
-    for i, ex in enumerate(a_ex):
-        if ex != []:
-            alpha_o = _excite(alpha_g, ex)
-        elif exc == "CUSTOM-PAIRED":
-            alpha_o, beta_o = alpha_g, _excite(beta_g, b_ex[i])
-        else:
-            break
+    for ex in a_ex:
+        alpha_o = _excite(alpha_g, ex)
         if exc in ("S", "SD", "HOMO-LUMO"):
             beta_o = beta_g
         if exc == "DOUBLE-PAIRED":
@@ -218,8 +214,6 @@ def excited_states(na, nb, norb, excitations=None, n_core=0, alpha_excitations=N
         states.append((list(alpha_o), list(beta_o)))
     if exc in ("S", "SD"):
         for ex in b_ex:
-            if ex == []:
-                break
             states.append((list(alpha_g), _excite(beta_g, ex)))
     if exc in ("D", "SD"):
         for ea in a_ex:

@@ -272,3 +272,28 @@ def test_ci_matrix_is_continuous_in_the_orbitals(name):
         H1, S1 = noci.noci_matrix(eng, pa, pb, na, nb)
         assert float((H1 - H0).abs().max()) < 1e-8
         assert float((S1 - S0).abs().max()) < 1e-10
+
+
+def _excitation_cases():
+    import json
+    with open(os.path.join(HERE, "golden", "excitation_lists.json")) as fh:
+        return json.load(fh)
+
+
+@pytest.mark.parametrize("case", _excitation_cases(),
+                         ids=lambda c: "%s-%s" % (c["molecule"], c["excitations"] or "custom"))
+def test_excitation_lists_match_reference(case):
+    """Every upstream excitation keyword on closed- and open-shell molecules
+    (make_golden_excitations.py): the state occupancies, the spin-flip list and the
+    core-orbital count; custom lists are rejected as upstream rejects them."""
+    if case.get("rejected"):
+        with pytest.raises(ValueError):
+            noci.excited_states(2, 2, 8, case["excitations"], alpha_excitations=case["alpha_excitations"],
+                                beta_excitations=case["beta_excitations"])
+        return
+    n_core = noci.n_core_orbitals([int(z) for z in case["charges"]])
+    assert n_core == case["n_core"]
+    states, sf = noci.excited_states(case["n_alpha"], case["n_beta"], case["n_orbitals"], case["excitations"],
+                                     n_core=n_core)
+    assert [[list(a), list(b)] for a, b in states] == case["states"]
+    assert [[i, list(a), list(b)] for i, a, b in sf] == case["spin_flip"]
