@@ -6,9 +6,12 @@ The input format is the reference's (``pychem.py:134-166``, ``Util/structures.py
 INI sections, every value a Python literal, strings case-insensitive.  Each section is
 one calculation; its results go to ``<section>.out`` next to the input and to stdout.
 
-Read keys: ``Method`` (HF, MP2), ``Reference`` (RHF, UHF, CUHF), ``Basis_Sets`` (the
-calculation runs in the last one; the upstream basis-fitting bootstrap through the
-earlier ones only supplies starting orbitals), ``Coords``, ``Coords_Units`` (ANGSTROM,
+Read keys: ``Method`` (HF, MP2), ``Reference`` (RHF, UHF, CUHF), ``Basis_Sets`` (each
+in turn, later ones seeded by orbitals fitted from the previous one as
+``pychem.py:96-117`` does; NOCI runs in the last one), ``SCF_Guess = "READ"`` with
+``MO_Read_Basis`` / ``MO_Read_State`` and ``Dump_MOs`` (MO text files
+``<basis>_<state>.alpha_MOs`` / ``.beta_MOs`` next to the input), ``Coords``,
+``Coords_Units`` (ANGSTROM,
 BOHR), ``Charge``, ``Multiplicity``, ``Max_SCF_Iterations``, ``Excitations`` (HOMO-LUMO:
 the alpha HOMO -> LUMO state by MOM after the ground state, as ``pychem.py:64-86``),
 ``Constrain_Excited``, ``Job_Type`` / ``Property_Type`` / ``Property_Grid``.
@@ -26,9 +29,12 @@ import sys
 
 import torch
 
+import numpy as np
+
 from . import noci, scattering
+from .basis_fit import fit_orbitals
 from .engine import GpuEngine
-from .molecule import Molecule
+from .molecule import Molecule, clean_basis_name
 from .scf import rhf, rmp2, uhf, ump2
 
 
@@ -54,8 +60,12 @@ def _coords(opts):
     return [[str(a[0]).upper(), float(a[1]), float(a[2]), float(a[3]), float(a[4])] for a in opts["COORDS"]], units
 
 
-def run_section(name, opts, write):
-    """One calculation; write(line) receives the report.  Returns a dict of results."""
+def run_section(name, opts, write, workdir="."):
+    """One calculation; write(line) receives the report.  Returns a dict of results.
+    MO text files (Dump_MOs, SCF_Guess = READ) live in ``workdir``."""
+    if not opts.get("METHOD", "HF").startswith("NOCI") and (
+            len(opts.get("BASIS_SETS", ["STO-3G"])) > 1 or opts.get("SCF_GUESS") == "READ" or opts.get("DUMP_MOS")):
+        return run_bootstrap(name, opts, write, workdir)
     method = opts.get("METHOD", "HF")
     ref = opts.get("REFERENCE", "RHF")
     basis = opts.get("BASIS_SETS", ["STO-3G"])[-1]
@@ -131,15 +141,142 @@ def _properties(mol, opts, densities, res, write):
         write("%10.6f" % S + "".join("%16.12f" % v for v in row))
 
 
+# ------------------------------------------------------------------------------------
+# Several basis sets, MO text files (pychem.py:62-117, hartree_fock.py:35-52,152-154)
+# ------------------------------------------------------------------------------------
+def _engine(mol):
+    return GpuEngine(mol).prepare()
+
+
+_rhf, _uhf, _rmp2, _ump2 = rhf, uhf, rmp2, ump2
+
+
+def mo_files(workdir, basis, state):
+    """Upstream's MO file names: <basis without punctuation>_<state>.alpha_MOs / .beta_MOs
+    (hartree_fock.py:152-154, structures.py:217-224)."""
+    stem = os.path.join(workdir, "%s_%s" % (clean_basis_name(basis), state))
+    return stem + ".alpha_MOs", stem + ".beta_MOs"
+
+
+def _read_mos(files, nbf, state):
+    fa, fb = files
+    try:
+        Ca, Cb = np.loadtxt(fa), np.loadtxt(fb)
+    except OSError:
+        raise FileNotFoundError("Could not read MO file for state %d (%s, %s)" % (state, fa, fb))
+    if Ca.ndim != 2 or Cb.ndim != 2 or len(Ca) != nbf or len(Cb) != nbf:
+        raise ValueError("Incorrect MOs supplied for state %d - check basis set and supply both alpha and beta sets"
+                         % state)
+    return Ca, Cb
+
+
+def run_bootstrap(name, opts, write, workdir="."):
+    """The state loop of pychem.py:62-117 over every listed basis set, for HF/MP2 with
+    the ground state and (UHF/CUHF, Excitations = HOMO-LUMO) its alpha HOMO -> LUMO
+    state.  First basis: the ground state from its own guess, or from MO files
+    (SCF_Guess = READ with MO_Read_Basis / MO_Read_State, hartree_fock.py:35-52), the
+    excited state from the ground state's orbitals with HOMO and LUMO swapped.  Each
+    later basis: orbitals of every state fitted from the previous basis
+    (pychem_gb300.basis_fit, basis_fit.py:6-21); the ground state restarts from its own
+    guess, the excited state starts from its fitted orbitals.  With Excitations given,
+    every state that starts from supplied orbitals keeps them occupied by MOM (upstream's
+    MOM switch, structures.py:289-305).  Dump_MOs writes every state's orbitals in every
+    basis (hartree_fock.py:152-154).  MP2 and properties use the last basis."""
+    method = opts.get("METHOD", "HF")
+    ref = opts.get("REFERENCE", "RHF")
+    bases = opts.get("BASIS_SETS", ["STO-3G"])
+    coords, units = _coords(opts)
+    charge, mult = int(opts.get("CHARGE", 0)), int(opts.get("MULTIPLICITY", 1))
+    max_iter = int(opts.get("MAX_SCF_ITERATIONS", 128))
+    exc = opts.get("EXCITATIONS")
+    use_mom = exc is not None
+    if exc not in (None, "HOMO-LUMO") or (exc == "HOMO-LUMO" and ref == "RHF"):
+        write("Excitations %s: not available in this build" % exc)
+    nstates = 2 if (exc == "HOMO-LUMO" and ref != "RHF") else 1
+    read = None
+    if opts.get("SCF_GUESS") == "READ":
+        st, rb = opts.get("MO_READ_STATE"), opts.get("MO_READ_BASIS")
+        if st is None or rb is None:
+            raise ValueError("Must give details of files to read alpha and beta MOs from, using keywords "
+                             "MO_Read_Basis and MO_Read_State")
+        read = [mo_files(workdir, rb, str(x)) for x in (st if isinstance(st, list) else [st])]
+    res = {"section": name, "reference": ref, "bases": list(bases), "per_basis": []}
+    fitted = None
+    for ib, basis in enumerate(bases):
+        mol = Molecule(coords, basis, charge=charge, multiplicity=mult, units=units)
+        eng = _engine(mol)
+        dev = eng.S.device
+        na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
+        write("Section %s: %s/%s %s, %d basis functions" % (name, ref, basis, method, mol.NOrbitals))
+        states = []
+        for k in range(nstates):
+            C0 = None
+            if ib == 0 and read is not None:
+                if k >= len(read):
+                    raise IndexError("No MO file given for state %d" % k)
+                C0 = _read_mos(read[k], mol.NOrbitals, k)
+            elif k > 0 and ib > 0:
+                C0 = fitted[k]
+            elif k > 0:
+                g = states[0]
+                Ca = g.Ca.clone()
+                Ca[:, [na - 1, na]] = Ca[:, [na, na - 1]]      # structures.reorder_MOs for HOMO -> LUMO
+                C0 = (Ca, g.Cb.clone())
+            if C0 is not None:
+                C0 = tuple(torch.as_tensor(np.asarray(c) if not torch.is_tensor(c) else c, dtype=torch.float64,
+                                           device=dev) for c in C0)
+            mom = use_mom and C0 is not None
+            if ref == "RHF":
+                D0 = None if C0 is None else C0[0][:, :na] @ C0[0][:, :na].T
+                r = _rhf(eng, max_iter=max_iter, D0=D0)
+            else:
+                r = _uhf(eng, cuhf=ref == "CUHF", max_iter=max(max_iter, 300), C0=C0, mom=mom,
+                         d_tol=1e-6 if mom else 1e-8)
+            states.append(r)
+            label = "ground" if k == 0 else "HOMO->LUMO (MOM)"
+            write("State %s: Final HF energy: %.11f (%d iterations%s)" % (label, r.E, r.iterations,
+                                                                           "" if r.converged else ", not converged"))
+            if opts.get("DUMP_MOS"):
+                Ca = r.C if ref == "RHF" else r.Ca
+                Cb = r.C if ref == "RHF" else r.Cb
+                fa, fb = mo_files(workdir, basis, k)
+                np.savetxt(fa, Ca.detach().cpu().numpy())
+                np.savetxt(fb, Cb.detach().cpu().numpy())
+        res["per_basis"].append({"basis": basis, "nbf": mol.NOrbitals,
+                                 "E_hf": [float(r.E) for r in states],
+                                 "iterations": [int(r.iterations) for r in states]})
+        if ib + 1 < len(bases):
+            nxt = bases[ib + 1]
+            fitted = []
+            for r in states:
+                Ca = (r.C if ref == "RHF" else r.Ca).detach().cpu().numpy()
+                Cb = (r.C if ref == "RHF" else r.Cb).detach().cpu().numpy()
+                fitted.append((fit_orbitals(mol, Ca, nxt), fit_orbitals(mol, Cb, nxt)))
+    res["basis"], res["nbf"] = bases[-1], mol.NOrbitals
+    res["states"] = []
+    for k, r in enumerate(states):
+        entry = {"label": "ground" if k == 0 else "HOMO->LUMO (MOM)", "E_hf": float(r.E),
+                 "iterations": int(r.iterations), "converged": bool(r.converged)}
+        if method.startswith("MP2"):
+            e2 = _rmp2(eng, r.C, r.eps) if ref == "RHF" else _ump2(eng, r)
+            entry["E_mp2_corr"] = e2
+            write("State %s: MP2 correlation energy: %.11f  Total MP2 energy: %.11f" % (entry["label"], e2,
+                                                                                       r.E + e2))
+        res["states"].append(entry)
+    _properties(mol, opts, [scattering.state_densities(r) for r in states], res, write)
+    return res
+
+
 def run_file(path, stream=sys.stdout):
     results = []
+    workdir = os.path.dirname(os.path.abspath(path))
     for name, opts in read_sections(path):
-        out_path = os.path.join(os.path.dirname(os.path.abspath(path)), name + ".out")
+        out_path = os.path.join(workdir, name + ".out")
         with open(out_path, "w") as fh:
             def write(line):
                 fh.write(line + "\n")
                 stream.write(line + "\n")
-            results.append(run_section(name, opts, write))
+            results.append(run_section(name, opts, write, workdir))
     return results
 
 
