@@ -348,17 +348,19 @@ def half_overlap(S):
     return (U[:, keep] * np.sqrt(s[keep])) @ U[:, keep].T
 
 
-def cuhf_constraint(S, Da, Db, Fa, Fb, na, nb):
+def cuhf_constraint(S, Da, Db, Fa, Fb, na, nb, spaces=None):
     """The CUHF constraint of Methods/hartree_fock.py:359-391 (constrain_UHF): natural
     orbitals from eigh(S^1/2 (D_tot / 2) S^1/2) with coefficients (S^1/2)^-1 V, and the
-    core-virtual block of (F_a - F_b) / 2 in that basis cancelled: F_a + L, F_b - L."""
+    core-virtual block of (F_a - F_b) / 2 in that basis cancelled: F_a + L, F_b - L.
+    spaces = (core, active): the counts of doubly and singly occupied positions of the
+    state's occupancy lists (hartree_fock.py:361-365); (nb, na - nb) for aufbau states."""
     Sh = half_overlap(S)
     P = Sh @ ((Da + Db) / 2.0) @ Sh
     vals, vecs = np.linalg.eigh(P)
     Cno = np.linalg.inv(Sh) @ vecs
     back = np.linalg.inv(Cno)
     idx = vals.argsort()[::-1]
-    nc, nact = nb, na - nb
+    nc, nact = spaces if spaces is not None else (nb, na - nb)
     core, virt = idx[:nc], idx[nc + nact:]
     delta = Cno.T @ ((Fa - Fb) / 2.0) @ Cno
     lam = np.zeros_like(delta)
@@ -410,7 +412,8 @@ def mom_order(C_new, e_new, C_ref, n, S):
     return C_new[:, order], e_new[order]
 
 
-def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1e-9, C0=None, mom=False):
+def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1e-9, C0=None, mom=False,
+        cuhf_spaces=None):
     """Unrestricted (or constrained, cuhf=True) Hartree-Fock along the upstream path of
     Methods/hartree_fock.py:23-142: core-Hamiltonian guess for both spins,
     F_s = H + J[D_a + D_b] - K[D_s] (hartree_fock.py:329-355), the optional CUHF
@@ -420,7 +423,8 @@ def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1
     density change below d_tol.  C0 = (Ca, Cb): starting orbitals (occupied columns
     first) instead of the core guess; mom: occupy by maximum overlap with C0's
     occupied orbitals (the FIXED reference of Methods/hf_extensions/mom.py) instead of
-    aufbau.  Returns dict(E, Ca, Cb, ea, eb, Da, Db, Fa, Fb, iterations, converged)."""
+    aufbau; cuhf_spaces: the constraint's (core, active) counts (cuhf_constraint).
+    Returns dict(E, Ca, Cb, ea, eb, Da, Db, Fa, Fb, iterations, converged)."""
     X = orthogonaliser(S)
     Xt = X.T
 
@@ -440,7 +444,7 @@ def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1
         Kb = np.einsum("cb,abcd->ad", Db, eri, optimize=True)
         Fa, Fb = H + J - Ka, H + J - Kb
         if cuhf:
-            Fa, Fb = cuhf_constraint(S, Da, Db, Fa, Fb, na, nb)
+            Fa, Fb = cuhf_constraint(S, Da, Db, Fa, Fb, na, nb, cuhf_spaces)
         return Fa, Fb
 
     def energy(Da, Db, Fa, Fb):

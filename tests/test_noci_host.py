@@ -147,8 +147,9 @@ def test_determinants_match_reference(name):
 
 
 class _Mol:
-    def __init__(self, e):
+    def __init__(self, e, na, nb):
         self.e = e
+        self.NAlphaElectrons, self.NBetaElectrons = na, nb
 
     def nuclear_repulsion(self):
         return self.e
@@ -161,7 +162,7 @@ class DenseEngine:
     def __init__(self, z):
         self.S, self.H = torch.tensor(z["S"]), torch.tensor(z["H"])
         self.eri = torch.tensor(z["eri_dense"])
-        self.mol = _Mol(float(z["E_nuc"]))
+        self.mol = _Mol(float(z["E_nuc"]), int(z["n_alpha"]), int(z["n_beta"]))
         self.nbf = self.S.shape[0]
 
     def coulomb_exchange(self, W):
@@ -297,3 +298,47 @@ def test_excitation_lists_match_reference(case):
                                      n_core=n_core)
     assert [[list(a), list(b)] for a, b in states] == case["states"]
     assert [[i, list(a), list(b)] for i, a, b in sf] == case["spin_flip"]
+
+
+def _oracle_uhf_for(z):
+    """The oracle's UHF in place of scf.uhf, with the occupation counts, starting
+    orbitals and CUHF spaces that hf_states passes."""
+    from pychem_gb300.scf import SCFResult
+    S, H, eri, e_nuc = z["S"], z["H"], z["eri_dense"], float(z["E_nuc"])
+
+    def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=False, occ=None,
+            cuhf_spaces=None):
+        na, nb = occ
+        c0 = None if C0 is None else (C0[0].numpy(), C0[1].numpy())
+        r = oracle.uhf(S, H, eri, na, nb, e_nuc, cuhf=cuhf, max_iter=max_iter, d_tol=d_tol, C0=c0, mom=mom,
+                       cuhf_spaces=cuhf_spaces)
+        Ca, Cb, ea, eb = r["Ca"], r["Cb"], r["ea"], r["eb"]
+        if mom:                                  # occupied orbitals by energy, as scf.uhf
+            for C, e, n in ((Ca, ea, na), (Cb, eb, nb)):
+                idx = np.argsort(e[:n], kind="stable")
+                C[:, :n], e[:n] = C[:, :n][:, idx], e[:n][idx]
+        return SCFResult(E=r["E"], Ca=torch.tensor(Ca), Cb=torch.tensor(Cb), ea=torch.tensor(ea),
+                         eb=torch.tensor(eb), iterations=r["iterations"], converged=r["converged"])
+    return uhf
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_state_scf_orchestration_against_reference(name, monkeypatch):
+    """noci.hf_states (state order, starting orbitals, MOM, constraints), determinants
+    and noci_matrix with the oracle's UHF and dense J/K: the reference's state
+    energies to 1e-7 and, where its algorithm defines them, its NOCI energies to 2e-5
+    (its MOM states stop on |dE| alone)."""
+    from scipy.linalg import eigh
+    z = load(name)
+    monkeypatch.setattr(noci, "uhf", _oracle_uhf_for(z))
+    eng = DenseEngine(z)
+    na, nb = int(z["n_alpha"]), int(z["n_beta"])
+    exc = str(z["excitations"])
+    states, sf = noci.excited_states(na, nb, z["S"].shape[0], exc)
+    res = noci.hf_states(eng, states, spin_flip="SF" in exc, reference="UHF", constrain_excited=True)
+    assert np.abs(np.array([r.E for r in res]) - z["hf_energies"]).max() < 1e-7
+    da, db = noci.determinants(states, res, sf if "SF" in exc else [])
+    H, S = noci.noci_matrix(eng, da, db, na, nb)
+    if energies_defined(z):
+        e = eigh(H.numpy(), S.numpy(), eigvals_only=True)
+        assert np.abs(e - z["noci_energies"]).max() < 2e-5
