@@ -34,7 +34,7 @@ import numpy as np
 from . import noci, scattering
 from .basis_fit import fit_orbitals
 from .engine import GpuEngine
-from .molecule import Molecule, clean_basis_name
+from .molecule import N_ELECTRONS, Molecule, clean_basis_name
 from .scf import rhf, rmp2, uhf, ump2
 
 
@@ -73,7 +73,7 @@ def run_section(name, opts, write, workdir="."):
     mol = Molecule(coords, basis, charge=int(opts.get("CHARGE", 0)), multiplicity=int(opts.get("MULTIPLICITY", 1)),
                    units=units)
     max_iter = int(opts.get("MAX_SCF_ITERATIONS", 128))
-    eng = GpuEngine(mol).prepare()
+    eng = _engine(mol)
     res = {"section": name, "basis": basis, "reference": ref, "nbf": mol.NOrbitals}
     write("Section %s: %s/%s %s, %d basis functions" % (name, ref, basis, method, mol.NOrbitals))
     if method.startswith("NOCI"):
@@ -99,6 +99,10 @@ def run_section(name, opts, write, workdir="."):
             raise ValueError("section %s: RHF needs a closed-shell molecule" % name)
         r = rhf(eng, max_iter=max_iter)
         states = [("ground", r)]
+        if opts.get("EXCITATIONS") is not None:
+            write("Excitations %s: excited states need Reference = UHF or CUHF in this build" % opts["EXCITATIONS"])
+    elif opts.get("EXCITATIONS") not in (None, "HOMO-LUMO"):
+        states = _excited_states(mol, eng, opts, ref, max_iter)
     else:
         r = uhf(eng, cuhf=ref == "CUHF", max_iter=max(max_iter, 300))
         states = [("ground", r)]
@@ -108,8 +112,6 @@ def run_section(name, opts, write, workdir="."):
             Ca[:, [na - 1, na]] = Ca[:, [na, na - 1]]      # structures.reorder_MOs for HOMO -> LUMO
             states.append(("HOMO->LUMO (MOM)", uhf(eng, cuhf=ref == "CUHF", C0=(Ca, r.Cb.clone()), mom=True,
                                                    max_iter=max(max_iter, 300), d_tol=1e-6)))
-        elif opts.get("EXCITATIONS") is not None:
-            write("Excitations %s: not available in this build" % opts["EXCITATIONS"])
     res["states"] = []
     for label, st in states:
         entry = {"label": label, "E_hf": st.E, "iterations": st.iterations, "converged": bool(st.converged)}
@@ -122,6 +124,25 @@ def run_section(name, opts, write, workdir="."):
         res["states"].append(entry)
     _properties(mol, opts, [scattering.state_densities(st) for _, st in states], res, write)
     return res
+
+
+def _excited_states(mol, eng, opts, ref, max_iter):
+    """Every state of an excitation keyword other than HOMO-LUMO (Util/structures.py:
+    526-657) by the state loop of pychem.py:62-93 (noci.hf_states): for spin-flip lists
+    the high-spin states first, each later state from its predecessor's orbitals and
+    held by MOM.  Labels give each state's occupied orbitals (alpha / beta)."""
+    exc = opts["EXCITATIONS"]
+    lists, _ = noci.excited_states(mol.NAlphaElectrons, mol.NBetaElectrons, mol.NOrbitals, exc,
+                                   n_core=noci.n_core_orbitals([N_ELECTRONS[a[0]] for a in mol.atoms]))
+    spin_flip = "SF" in noci.EXCITATION_ALIASES.get(exc, exc)
+    res = noci.hf_states(eng, lists, spin_flip=spin_flip, reference=ref,
+                         constrain_excited=bool(opts.get("CONSTRAIN_EXCITED", ref == "CUHF")),
+                         max_iter=max(max_iter, 300))
+
+    def occupied(o):
+        return ",".join(str(i) for i, x in enumerate(o) if x)
+
+    return [("%d [%s / %s]" % (k, occupied(a), occupied(b)), r) for k, ((a, b), r) in enumerate(zip(lists, res))]
 
 
 def _properties(mol, opts, densities, res, write):

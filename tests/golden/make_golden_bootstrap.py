@@ -5,9 +5,9 @@ default ``/root/reference``):
 
     python tests/golden/make_golden_bootstrap.py
 
-Each case runs ``pychem.do_calculation`` with several ``Basis_Sets``: the states in
-the first basis, then for every later basis the orbitals fitted by
-``Methods/basis_fit.py`` and the states again (``pychem.py:62-117``).  Every
+Each case runs ``pychem.do_calculation``: the states of its excitation keyword in the
+first basis (``pychem.py:62-93``), then for every later basis the orbitals fitted by
+``Methods/basis_fit.py`` and the states again (``pychem.py:96-117``).  Every
 ``hartree_fock.do`` call is wrapped to record (basis, state, final energy, orbitals);
 ``bootstrap.json`` holds the energies, ``bootstrap.npz`` the orbitals.  The geometries
 are this project's own.
@@ -35,6 +35,9 @@ H2 = [["H", 1.0, 0.0, 0.0, 0.0], ["H", 1.0, 0.74, 0.0, 0.0]]
 LIH = [["Li", 3.0, 0.0, 0.0, 0.0], ["H", 1.0, 1.6, 0.0, 0.0]]
 CASES = [
     # name, coords, bases, reference, excitations
+    ("states_lih_singles_sto3g", LIH, ["STO-3G"], "UHF", "SINGLES"),
+    ("states_h2_sd_631g", H2, ["6-31G"], "UHF", "SINGLES-DOUBLES"),
+    ("states_lih_sfs_hf_sto3g", LIH, ["STO-3G"], "UHF", "SFS"),
     ("boot_h2_mom_sto3g_631g", H2, ["STO-3G", "6-31G"], "UHF", "HOMO-LUMO"),
     ("boot_h2_mom_sto3g_ccpvdz", H2, ["STO-3G", "cc-pVDZ"], "UHF", "HOMO-LUMO"),
     ("boot_lih_mom_sto3g_631g", LIH, ["STO-3G", "6-31G"], "UHF", "HOMO-LUMO"),
