@@ -35,7 +35,7 @@ from . import noci, scattering
 from .basis_fit import fit_orbitals
 from .engine import GpuEngine
 from .molecule import N_ELECTRONS, Molecule, clean_basis_name
-from .scf import rhf, rmp2, uhf, ump2
+from .scf import MP2_SCALES, rhf, rmp2, uhf, ump2
 
 
 def read_sections(path):
@@ -118,7 +118,8 @@ def run_section(name, opts, write, workdir="."):
         write("State %s: Final HF energy: %.11f (%d iterations%s)" % (label, st.E, st.iterations,
                                                                        "" if st.converged else ", not converged"))
         if method.startswith("MP2"):
-            e2 = rmp2(eng, st.C, st.eps) if ref == "RHF" else ump2(eng, st)
+            sc = MP2_SCALES.get(method)
+            e2 = rmp2(eng, st.C, st.eps, scale=sc) if ref == "RHF" else ump2(eng, st, scale=sc)
             entry["E_mp2_corr"] = e2
             write("State %s: MP2 correlation energy: %.11f  Total MP2 energy: %.11f" % (label, e2, st.E + e2))
         res["states"].append(entry)
@@ -279,7 +280,8 @@ def run_bootstrap(name, opts, write, workdir="."):
         entry = {"label": "ground" if k == 0 else "HOMO->LUMO (MOM)", "E_hf": float(r.E),
                  "iterations": int(r.iterations), "converged": bool(r.converged)}
         if method.startswith("MP2"):
-            e2 = _rmp2(eng, r.C, r.eps) if ref == "RHF" else _ump2(eng, r)
+            sc = MP2_SCALES.get(method)
+            e2 = _rmp2(eng, r.C, r.eps, scale=sc) if ref == "RHF" else _ump2(eng, r, scale=sc)
             entry["E_mp2_corr"] = e2
             write("State %s: MP2 correlation energy: %.11f  Total MP2 energy: %.11f" % (entry["label"], e2,
                                                                                        r.E + e2))

@@ -246,9 +246,14 @@ def mp2_transform(eri, Co, Cv, gemm="ozaki", nslice=6, Co2=None, Cv2=None):
     return T.reshape(o, v, o2, v2)
 
 
-def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6):
+MP2_SCALES = {"MP2": None, "MP2-SCS": (1.0 / 3.0, 6.0 / 5.0), "MP2-SOS": (0.0, 1.3)}   # Methods/mp2.py:97-107
+
+
+def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6, scale=None):
     """Closed-shell MP2 correlation energy: four quarter transforms of the dense AO
-    tensor to (ia|jb) and the energy denominator sum."""
+    tensor to (ia|jb) and the energy denominator sum.  scale = (c_ss, c_os) weights
+    the same-spin part sum (ia|jb)((ia|jb) - (ib|ja))/D and the opposite-spin part
+    sum (ia|jb)^2/D (MP2_SCALES: SCS and SOS as Methods/mp2.py:97-107)."""
     mol = engine.mol
     o = mol.NAlphaElectrons
     if eri is None:
@@ -258,6 +263,11 @@ def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6):
     ovov = mp2_transform(eri, Co, Cv, gemm=gemm, nslice=nslice)
     eo, ev = eps[:o], eps[o:]
     den = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
+    if scale is not None:
+        t = ovov / den
+        e_os = torch.sum(ovov * t)
+        e_ss = torch.sum((ovov - ovov.permute(0, 3, 2, 1)) * t)
+        return float(scale[0] * e_ss + scale[1] * e_os)
     e2 = torch.sum(ovov * (2.0 * ovov - ovov.permute(0, 3, 2, 1)) / den)
     return float(e2)
 
@@ -426,11 +436,12 @@ def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=
                      converged=converged)
 
 
-def ump2(engine, res, eri=None, gemm="ozaki", nslice=6):
+def ump2(engine, res, eri=None, gemm="ozaki", nslice=6, scale=None):
     """Unrestricted MP2 correlation energy (Methods/mp2.py:43-101): same-spin
     0.25 sum ((ia|jb) - (ib|ja))^2 / D per spin and opposite-spin sum (ia|jb)^2 / D,
     with the orbital energies of the final Fock matrices; the integrals from the four
-    quarter transforms of mp2_transform."""
+    quarter transforms of mp2_transform.  scale = (c_ss, c_os) weights the same-spin
+    and opposite-spin parts (MP2_SCALES)."""
     mol = engine.mol
     na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
     if eri is None:
@@ -453,4 +464,6 @@ def ump2(engine, res, eri=None, gemm="ozaki", nslice=6):
         den = (ea[:na, None, None, None] - ea[None, na:, None, None] + eb[None, None, :nb, None]
                - eb[None, None, None, nb:])
         e_ab = float(torch.sum(g * g / den))
+    if scale is not None:
+        return scale[0] * (same(Ca, ea, na) + same(Cb, eb, nb)) + scale[1] * e_ab
     return same(Ca, ea, na) + same(Cb, eb, nb) + e_ab
