@@ -98,8 +98,9 @@ def boys(mmax, T):
 class Basis:
     """Shells of a molecule in upstream AO order."""
 
-    def __init__(self, atoms, basis_name):
-        """atoms: list of (symbol, Z, x, y, z) with coordinates in bohr."""
+    def __init__(self, atoms, basis_name, max_l=None):
+        """atoms: list of (symbol, Z, x, y, z) with coordinates in bohr; max_l drops the
+        shells above that angular momentum (Util/structures.py:815-826)."""
         with open(BASIS_JSON) as fh:
             lib_sets = json.load(fh)
         key = basis_name.replace("*", "s").replace("-", "").replace("(", "").replace(")", "").replace(",", "").upper()
@@ -109,6 +110,8 @@ class Basis:
         for ia, (sym, Z, xyz) in enumerate(self.atoms):
             for fn in data[sym]:
                 l = fn[0]
+                if max_l is not None and l > max_l:
+                    continue
                 exps = np.array([p[0] for p in fn[1:]], dtype=float)
                 ccs = np.array([p[1] for p in fn[1:]], dtype=float)
                 self.shells.append((l, exps, ccs, xyz, ia))

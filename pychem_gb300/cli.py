@@ -14,7 +14,11 @@ in turn, later ones seeded by orbitals fitted from the previous one as
 ``Coords_Units`` (ANGSTROM,
 BOHR), ``Charge``, ``Multiplicity``, ``Max_SCF_Iterations``, ``Excitations`` (HOMO-LUMO:
 the alpha HOMO -> LUMO state by MOM after the ground state, as ``pychem.py:64-86``),
-``Constrain_Excited``, ``Job_Type`` / ``Property_Type`` / ``Property_Grid``.
+``Constrain_Excited``, ``Job_Type`` / ``Property_Type`` / ``Property_Grid``, ``Max_L``
+(shells above it dropped).  ``Cartesian_L``, ``MOM_Reference = "MUTABLE"`` and
+``Use_MOM = False`` with excited states stop the section with ValueError (not
+implemented); printing and DIIS tuning keys are read by upstream only for output
+detail and its own SCF loop, and are ignored here.
 ``Method = "NOCI"`` runs the states of any ``Excitations`` keyword (spin-flip lists
 included) and the NOCI of ``Methods/noci.py`` (pychem_gb300.noci).
 ``Job_Type = "PROPERTY"`` with ``Property_Type = "SCATTERING"`` adds the total
@@ -60,6 +64,18 @@ def _coords(opts):
     return [[str(a[0]).upper(), float(a[1]), float(a[2]), float(a[3]), float(a[4])] for a in opts["COORDS"]], units
 
 
+def _check_options(opts):
+    """Input keys of the reference that change the model in ways this build does not
+    implement stop the section instead of being ignored."""
+    if opts.get("CARTESIAN_L"):
+        raise ValueError("Cartesian basis functions (Cartesian_L = %r) are not available in this build: every shell "
+                         "is spherical" % (opts["CARTESIAN_L"],))
+    if opts.get("MOM_REFERENCE") == "MUTABLE":
+        raise ValueError("MOM_Reference = MUTABLE is not available in this build (FIXED is)")
+    if opts.get("USE_MOM") is False and opts.get("EXCITATIONS") is not None:
+        raise ValueError("Use_MOM = False with excited states is not available in this build")
+
+
 def run_section(name, opts, write, workdir="."):
     """One calculation; write(line) receives the report.  Returns a dict of results.
     MO text files (Dump_MOs, SCF_Guess = READ) live in ``workdir``."""
@@ -70,8 +86,9 @@ def run_section(name, opts, write, workdir="."):
     ref = opts.get("REFERENCE", "RHF")
     basis = opts.get("BASIS_SETS", ["STO-3G"])[-1]
     coords, units = _coords(opts)
+    _check_options(opts)
     mol = Molecule(coords, basis, charge=int(opts.get("CHARGE", 0)), multiplicity=int(opts.get("MULTIPLICITY", 1)),
-                   units=units)
+                   units=units, max_l=opts.get("MAX_L"))
     max_iter = int(opts.get("MAX_SCF_ITERATIONS", 128))
     eng = _engine(mol)
     res = {"section": name, "basis": basis, "reference": ref, "nbf": mol.NOrbitals}
@@ -204,6 +221,7 @@ def run_bootstrap(name, opts, write, workdir="."):
     every state that starts from supplied orbitals keeps them occupied by MOM (upstream's
     MOM switch, structures.py:289-305).  Dump_MOs writes every state's orbitals in every
     basis (hartree_fock.py:152-154).  MP2 and properties use the last basis."""
+    _check_options(opts)
     method = opts.get("METHOD", "HF")
     ref = opts.get("REFERENCE", "RHF")
     bases = opts.get("BASIS_SETS", ["STO-3G"])
@@ -225,7 +243,7 @@ def run_bootstrap(name, opts, write, workdir="."):
     res = {"section": name, "reference": ref, "bases": list(bases), "per_basis": []}
     fitted = None
     for ib, basis in enumerate(bases):
-        mol = Molecule(coords, basis, charge=charge, multiplicity=mult, units=units)
+        mol = Molecule(coords, basis, charge=charge, multiplicity=mult, units=units, max_l=opts.get("MAX_L"))
         eng = _engine(mol)
         dev = eng.S.device
         na, nb = mol.NAlphaElectrons, mol.NBetaElectrons

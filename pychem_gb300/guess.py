@@ -35,15 +35,16 @@ def _fractional_occupations(eps, nelec_alpha, degeneracy_tol=1e-3):
     return out
 
 
-def atomic_density(symbol, Z, basis, device="cuda", iters=40, damping=0.5):
-    """Alpha density of a free atom (fractional occupation, spin averaged)."""
-    key = (symbol.upper(), basis, str(device))
+def atomic_density(symbol, Z, basis, device="cuda", iters=40, damping=0.5, max_l=None):
+    """Alpha density of a free atom (fractional occupation, spin averaged); max_l: the
+    molecule's shell cut (Molecule.max_l)."""
+    key = (symbol.upper(), basis, str(device), max_l)
     if key in _ATOM_CACHE:
         return _ATOM_CACHE[key]
     from .engine import GpuEngine
     from .molecule import N_ELECTRONS, Molecule
     ne = N_ELECTRONS[symbol.upper()]
-    mol = Molecule([[symbol, Z, 0.0, 0.0, 0.0]], basis, multiplicity=1 + (ne % 2))
+    mol = Molecule([[symbol, Z, 0.0, 0.0, 0.0]], basis, multiplicity=1 + (ne % 2), max_l=max_l)
     eng = GpuEngine(mol, device=device).prepare()
     S, H = eng.S, eng.H
     s, U = eigen.eigh(S)
@@ -74,7 +75,7 @@ def sad_density(mol, device="cuda"):
     ao = 0
     first_shell = 0
     for ia, (sym, Z, _) in enumerate(mol.atoms):
-        Da = atomic_density(sym, Z, mol.Basis, device)
+        Da = atomic_density(sym, Z, mol.Basis, device, max_l=getattr(mol, "max_l", None))
         na = Da.shape[0]
         D[ao:ao + na, ao:ao + na] = Da
         ao += na

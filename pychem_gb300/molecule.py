@@ -67,7 +67,7 @@ def pure_norm(l):
 
 
 class Molecule:
-    def __init__(self, coords, basis="STO-3G", charge=0, multiplicity=1, units="ANGSTROM"):
+    def __init__(self, coords, basis="STO-3G", charge=0, multiplicity=1, units="ANGSTROM", max_l=None):
         scale = TO_BOHR if units.upper() == "ANGSTROM" else 1.0
         self.Basis = clean_basis_name(basis)
         lib = basis_library()
@@ -75,6 +75,7 @@ class Molecule:
             raise ValueError("basis set %s not available (have %s)" % (basis, sorted(lib)))
         self.Charge = charge
         self.Multiplicity = multiplicity
+        self.max_l = max_l
         self.atoms = []
         for row in coords:
             sym = str(row[0]).upper()
@@ -82,7 +83,9 @@ class Molecule:
         self.NAtom = len(self.atoms)
         shells = []
         for ia, (sym, Z, xyz) in enumerate(self.atoms):
-            shells += [(l, exps, ccs, ia) for l, exps, ccs in element_shells(self.Basis, sym)]
+            # max_l: upstream's Max_L, the shells above it dropped (Util/structures.py:815-826)
+            shells += [(l, exps, ccs, ia) for l, exps, ccs in element_shells(self.Basis, sym)
+                       if max_l is None or l <= max_l]
         self.shells = shells
         self.NCgtf = len(shells)
         ao = 0
