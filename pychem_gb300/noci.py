@@ -253,7 +253,7 @@ def hf_states(engine, states, spin_flip=False, reference="UHF", constrain_excite
     reference, and to the excited ones with constrain_excited (hartree_fock.py:99).
     Returns one SCFResult per state, in state order."""
     if reference not in ("UHF", "CUHF"):
-        raise ValueError("NOCI states need a UHF or CUHF reference")
+        raise ValueError("excited and spin-flip states need a UHF or CUHF reference")
     mol = engine.mol
     order = list(range(len(states)))
     if spin_flip:
