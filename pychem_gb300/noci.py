@@ -394,20 +394,46 @@ def _pair(C1, C2, S, n):
     return A2, torch.where(flip.unsqueeze(1), -B2, B2)
 
 
-def noci_matrix(engine, dets_a, dets_b, na, nb, return_pairs=False):
+def noci_matrix(engine, dets_a, dets_b, na, nb, return_pairs=False, max_pairs=None):
     """CI Hamiltonian and overlap over the determinants (lower triangle with the
     row's determinant as the bra, mirrored), as Methods/noci.py:55-106, without a
     host round trip: zero-overlap cases are masks, the first zero's orbital pair a
     column gather, and the J/K of all pairs' co-densities one batched digestion.
-    With return_pairs, also the lower-triangle indices and the paired orbitals
-    (a1, a2, b1, b2), one row per pair."""
-    S, H = engine.S, engine.H
+    Pairs are evaluated in chunks of at most max_pairs (default: about 2 GB of
+    per-pair matrices).  With return_pairs, also the lower-triangle indices and the
+    paired orbitals (a1, a2, b1, b2), one row per pair."""
+    S = engine.S
     e_nuc = engine.mol.nuclear_repulsion()
     m = len(dets_a)
     dev = S.device
     f64 = torch.float64
+    nbf = S.shape[0]
     ii, jj = torch.tril_indices(m, m, device=dev).unbind(0)
     Da, Db = torch.stack(dets_a), torch.stack(dets_b)
+    P = ii.numel()
+    if max_pairs is None:
+        max_pairs = max(1, int(2.0e9 // (96 * nbf * nbf)))
+    parts = [_pair_elements(engine, Da, Db, ii[k:k + max_pairs], jj[k:k + max_pairs], na, nb, e_nuc)
+             for k in range(0, P, max_pairs)]
+    hval = torch.cat([x[0] for x in parts])
+    s_state = torch.cat([x[1] for x in parts])
+    Hci = torch.zeros(m, m, dtype=f64, device=dev)
+    Sci = torch.zeros_like(Hci)
+    Hci[ii, jj] = hval
+    Hci[jj, ii] = hval
+    Sci[ii, jj] = s_state
+    Sci[jj, ii] = s_state
+    if return_pairs:
+        return Hci, Sci, (ii, jj) + tuple(torch.cat([x[k] for x in parts]) for k in range(2, 6))
+    return Hci, Sci
+
+
+def _pair_elements(engine, Da, Db, ii, jj, na, nb, e_nuc):
+    """Elements and overlaps of the pairs (ii[p], jj[p]) (noci.py:63-106); returns
+    (H values, overlaps, a1, a2, b1, b2)."""
+    S, H = engine.S, engine.H
+    dev = S.device
+    f64 = torch.float64
     P, nbf = ii.numel(), S.shape[0]
     empty = torch.zeros(P, nbf, 0, dtype=f64, device=dev)
     a1, a2 = _pair(Da[ii], Da[jj], S, na) if na else (empty, empty)
@@ -462,15 +488,7 @@ def noci_matrix(engine, dets_a, dets_b, na, nb, return_pairs=False):
     e12 = e12 + torch.where(one, torch.where(spin_a, zc_a, zc_b), 0.0)
     elem = torch.where(nz == 0, e0, torch.where(nz <= 2, e12, 0.0))
     hval = elem * reduced + e_nuc * s_state
-    Hci = torch.zeros(m, m, dtype=f64, device=dev)
-    Sci = torch.zeros_like(Hci)
-    Hci[ii, jj] = hval
-    Hci[jj, ii] = hval
-    Sci[ii, jj] = s_state
-    Sci[jj, ii] = s_state
-    if return_pairs:
-        return Hci, Sci, (ii, jj, a1, a2, b1, b2)
-    return Hci, Sci
+    return hval, s_state, a1, a2, b1, b2
 
 
 def generalized_eigh(Hci, Sci):

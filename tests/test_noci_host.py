@@ -342,3 +342,18 @@ def test_state_scf_orchestration_against_reference(name, monkeypatch):
     if energies_defined(z):
         e = eigh(H.numpy(), S.numpy(), eigvals_only=True)
         assert np.abs(e - z["noci_energies"]).max() < 2e-5
+
+
+def test_ci_matrix_in_chunks_equals_one_pass():
+    """noci_matrix evaluates pairs in bounded chunks; any chunking gives the same
+    matrices and paired orbitals."""
+    z = load("noci_c2_sfd_cisd_631g")
+    eng = DenseEngine(z)
+    na, nb = int(z["n_alpha"]), int(z["n_beta"])
+    da = [torch.tensor(x) for x in z["det_alpha"]]
+    db = [torch.tensor(x) for x in z["det_beta"]]
+    H1, S1, p1 = noci.noci_matrix(eng, da, db, na, nb, return_pairs=True)
+    H2, S2, p2 = noci.noci_matrix(eng, da, db, na, nb, return_pairs=True, max_pairs=37)
+    assert float((H1 - H2).abs().max()) < 1e-12 and float((S1 - S2).abs().max()) < 1e-14
+    for x, y in zip(p1, p2):
+        assert x.shape == y.shape and float((x.double() - y.double()).abs().max()) < 1e-12
