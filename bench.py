@@ -11,6 +11,13 @@ energy.  `value` is the time of that step (time-to-convergence incl. MP2, second
 CUDA events, L2 flushed between steps); `e2e` is the same solve through the public
 call pychem_gb300.api.rhf_mp2 from host coordinates to host results.
 
+Extra keys on the same line (rank 0, N = 1): ``mixed`` (mixed-precision ERIs on the
+same workload), ``alkane_mixed`` (C12H26 / cc-pVDZ), ``ensemble`` (1024 molecules,
+batched SCF), ``learned_guess`` (learned initial densities on 1024 held-out molecules),
+``noci_spin_flip`` (spin-flip NOCI, C2 / cc-pVDZ, 27 determinants) and ``scattering``
+(electron-scattering intensities, (H2O)8 / 6-31G, 16 grid values), each with the CPU
+oracle's time on a bounded sample where it has one.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
 import argparse
