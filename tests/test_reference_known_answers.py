@@ -162,3 +162,16 @@ def test_scattering_examples_at_zero_momentum(example):
     for S, printed in tab:
         I = oracle.scattering_intensity(r["D"], r["D"], b.eri_dense(scattering=S), mol.NElectrons)
         assert abs(I - printed) < 1e-10
+
+
+def test_example3_cuhf_energy():
+    """Tests/example3 (CUHF, 6-311G): the printed final Hartree-Fock energy against the
+    oracle's CUHF, within the 3e-6 that the reference's |dE| < 1e-7 stop leaves."""
+    (name, opts), = cli.read_sections(os.path.join(TESTS, "example3.inp"))
+    assert opts["REFERENCE"] == "CUHF"
+    mol = molecule(opts)
+    eng = CpuEngine(mol)
+    r = oracle.uhf(eng.S.numpy(), eng.H.numpy(), eng.eri, mol.NAlphaElectrons, mol.NBetaElectrons, eng.e_nuc,
+                   cuhf=True)
+    printed = re.findall(r"Final HF energy:\s*([-0-9.eE+]+)", open(os.path.join(TESTS, "example3.out")).read())
+    assert printed and abs(r["E"] - float(printed[-1])) < 3e-6
