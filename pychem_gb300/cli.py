@@ -6,34 +6,36 @@ The input format is the reference's (``pychem.py:134-166``, ``Util/structures.py
 INI sections, every value a Python literal, strings case-insensitive.  Each section is
 one calculation; its results go to ``<section>.out`` next to the input and to stdout.
 
-Read keys: ``Method`` (HF, MP2), ``Reference`` (RHF, UHF, CUHF), ``Basis_Sets`` (each
-in turn, later ones seeded by orbitals fitted from the previous one as
-``pychem.py:96-117`` does; NOCI runs in the last one), ``SCF_Guess = "READ"`` with
-``MO_Read_Basis`` / ``MO_Read_State`` and ``Dump_MOs`` (MO text files
-``<basis>_<state>.alpha_MOs`` / ``.beta_MOs`` next to the input), ``Coords``,
-``Coords_Units`` (ANGSTROM,
-BOHR), ``Charge``, ``Multiplicity``, ``Max_SCF_Iterations``, ``Excitations`` (HOMO-LUMO:
-the alpha HOMO -> LUMO state by MOM after the ground state, as ``pychem.py:64-86``),
-``Constrain_Excited``, ``Job_Type`` / ``Property_Type`` / ``Property_Grid``, ``Max_L``
-(shells above it dropped).  ``Cartesian_L``, ``MOM_Reference = "MUTABLE"`` and
-``Use_MOM = False`` with excited states stop the section with ValueError (not
-implemented); printing and DIIS tuning keys are read by upstream only for output
-detail and its own SCF loop, and are ignored here.
-``Method = "NOCI"`` runs the states of any ``Excitations`` keyword (spin-flip lists
-included) and the NOCI of ``Methods/noci.py`` (pychem_gb300.noci).
-``Job_Type = "PROPERTY"`` with ``Property_Type = "SCATTERING"`` adds the total
-electron-scattering intensity of every state at every grid value
-(``Methods/properties.py:6-37``, pychem_gb300.scattering), after NOCI of its
-determinants as upstream.
+Keys read:
+
+* ``Method``: HF, MP2, MP2-SCS, MP2-SOS (spin-component scaling of
+  ``Methods/mp2.py:97-107``), NOCI (and NOCI-P2 variants, which upstream runs as NOCI).
+* ``Reference``: RHF, UHF, CUHF; ``Constrain_Excited``.
+* ``Coords``, ``Coords_Units`` (ANGSTROM, BOHR), ``Charge``, ``Multiplicity``,
+  ``Max_SCF_Iterations``, ``Max_L`` (shells above it dropped).
+* ``Basis_Sets``: each in turn, later ones seeded by orbitals fitted from the previous
+  one (``pychem.py:96-117``, pychem_gb300.basis_fit); NOCI runs in the last one.
+* ``Excitations``: any upstream keyword (``Util/structures.py:393-413``); HOMO-LUMO by
+  MOM from the ground state (``pychem.py:64-86``), the others through the state loop of
+  pychem_gb300.noci.hf_states, spin-flip lists included.
+* ``SCF_Guess = "READ"`` with ``MO_Read_Basis`` / ``MO_Read_State``, and ``Dump_MOs``:
+  MO text files ``<basis>_<state>.alpha_MOs`` / ``.beta_MOs`` next to the input.
+* ``Job_Type = "PROPERTY"`` with ``Property_Type = "SCATTERING"`` and
+  ``Property_Grid``: the total electron-scattering intensity of every state at every
+  grid value (``Methods/properties.py:6-37``, pychem_gb300.scattering), after NOCI of
+  its determinants as upstream.
+
+``Cartesian_L``, ``MOM_Reference = "MUTABLE"`` and ``Use_MOM = False`` with excited
+states stop the section with ValueError (not implemented).  Printing and DIIS tuning
+keys only shape upstream's output and its own SCF loop, and are ignored.
 """
 import ast
 import configparser
 import os
 import sys
 
-import torch
-
 import numpy as np
+import torch
 
 from . import noci, scattering
 from .basis_fit import fit_orbitals
