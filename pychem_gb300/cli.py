@@ -120,7 +120,9 @@ def run_section(name, opts, write, workdir="."):
         states = [("ground", r)]
         if opts.get("EXCITATIONS") is not None:
             write("Excitations %s: excited states need Reference = UHF or CUHF in this build" % opts["EXCITATIONS"])
-    elif opts.get("EXCITATIONS") not in (None, "HOMO-LUMO"):
+    elif opts.get("EXCITATIONS") not in (None, "HOMO-LUMO") or (
+            opts.get("EXCITATIONS") == "HOMO-LUMO" and (ref == "CUHF" or opts.get("CONSTRAIN_EXCITED"))):
+        # constrained excited states need the occupancy's CUHF spaces (hf_states)
         states = _excited_states(mol, eng, opts, ref, max_iter)
     else:
         r = uhf(eng, cuhf=ref == "CUHF", max_iter=max(max_iter, 300))
@@ -242,6 +244,7 @@ def run_bootstrap(name, opts, write, workdir="."):
             raise ValueError("Must give details of files to read alpha and beta MOs from, using keywords "
                              "MO_Read_Basis and MO_Read_State")
         read = [mo_files(workdir, rb, str(x)) for x in (st if isinstance(st, list) else [st])]
+    constrain_excited = bool(opts.get("CONSTRAIN_EXCITED", ref == "CUHF"))
     res = {"section": name, "reference": ref, "bases": list(bases), "per_basis": []}
     fitted = None
     for ib, basis in enumerate(bases):
@@ -272,8 +275,15 @@ def run_bootstrap(name, opts, write, workdir="."):
                 D0 = None if C0 is None else C0[0][:, :na] @ C0[0][:, :na].T
                 r = _rhf(eng, max_iter=max_iter, D0=D0)
             else:
-                r = _uhf(eng, cuhf=ref == "CUHF", max_iter=max(max_iter, 300), C0=C0, mom=mom,
-                         d_tol=1e-6 if mom else 1e-8)
+                # CUHF spaces from the state's occupancy (hartree_fock.py:361-365): the
+                # HOMO -> LUMO state has two singly occupied positions
+                n = mol.NOrbitals
+                occ_a = [1] * na + [0] * (n - na)
+                if k > 0:
+                    occ_a[na - 1], occ_a[na] = 0, 1
+                tot = [a + (1 if i < nb else 0) for i, a in enumerate(occ_a)]
+                r = _uhf(eng, cuhf=ref == "CUHF" or (constrain_excited and k > 0), max_iter=max(max_iter, 300),
+                         C0=C0, mom=mom, d_tol=1e-6 if mom else 1e-8, cuhf_spaces=(tot.count(2), tot.count(1)))
             states.append(r)
             label = "ground" if k == 0 else "HOMO->LUMO (MOM)"
             write("State %s: Final HF energy: %.11f (%d iterations%s)" % (label, r.E, r.iterations,

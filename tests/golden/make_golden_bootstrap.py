@@ -42,7 +42,10 @@ CASES = [
     ("boot_h2_mom_sto3g_ccpvdz", H2, ["STO-3G", "cc-pVDZ"], "UHF", "HOMO-LUMO"),
     ("boot_lih_mom_sto3g_631g", LIH, ["STO-3G", "6-31G"], "UHF", "HOMO-LUMO"),
     ("boot_h2o_rhf_sto3g_631g_ccpvdz", water(), ["STO-3G", "6-31G", "cc-pVDZ"], "RHF", None),
+    ("boot_lih_mom_constrained_sto3g_631g", LIH, ["STO-3G", "6-31G"], "UHF", "HOMO-LUMO"),
+    ("states_h2o_homo_lumo_constrained_sto3g", water(), ["STO-3G"], "UHF", "HOMO-LUMO"),
 ]
+CONSTRAINED = {"boot_lih_mom_constrained_sto3g_631g", "states_h2o_homo_lumo_constrained_sto3g"}
 
 
 def main():
@@ -71,6 +74,8 @@ def main():
             extra = {"Max_SCF_Iterations": 300}
             if exc:
                 extra["Excitations"] = exc
+            if name in CONSTRAINED:
+                extra["Constrain_Excited"] = True
             mol, st = refrun.molecule_from_spec(ns, coords, bases[0], reference=ref, extra=extra)
             st.BasisSets = [b.replace("-", "").upper() for b in bases]
             st.OutFileName = name + ".out"
@@ -78,6 +83,7 @@ def main():
             hf.do = do
             pychem.hartree_fock.do = do
             summary[name] = {"bases": bases, "reference": ref, "excitations": exc, "coords": coords,
+                             "constrain_excited": name in CONSTRAINED,
                              "calls": [[c[0], c[1], c[2]] for c in calls]}
             for k, c in enumerate(calls):
                 arrays["%s_%d_alpha" % (name, k)] = c[3]

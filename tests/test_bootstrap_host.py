@@ -54,11 +54,11 @@ def oracle_rhf(eng, max_iter=128, D0=None, **kw):
                      iterations=r["iterations"], converged=r["converged"])
 
 
-def oracle_uhf(eng, cuhf=False, max_iter=300, C0=None, mom=False, d_tol=1e-8, **kw):
+def oracle_uhf(eng, cuhf=False, max_iter=300, C0=None, mom=False, d_tol=1e-8, cuhf_spaces=None, **kw):
     m = eng.mol
     c0 = None if C0 is None else (C0[0].numpy(), C0[1].numpy())
     r = oracle.uhf(eng.S.numpy(), eng.H.numpy(), eng.eri, m.NAlphaElectrons, m.NBetaElectrons, eng.e_nuc,
-                   cuhf=cuhf, max_iter=max_iter, C0=c0, mom=mom, d_tol=d_tol)
+                   cuhf=cuhf, max_iter=max_iter, C0=c0, mom=mom, d_tol=d_tol, cuhf_spaces=cuhf_spaces)
     return SCFResult(E=r["E"], Ca=torch.tensor(r["Ca"]), Cb=torch.tensor(r["Cb"]), ea=torch.tensor(r["ea"]),
                      eb=torch.tensor(r["eb"]), Da=torch.tensor(r["Da"]), Db=torch.tensor(r["Db"]),
                      iterations=r["iterations"], converged=r["converged"])
@@ -75,7 +75,8 @@ def oracle_runner(monkeypatch):
 def _opts(case):
     return {"METHOD": "HF", "REFERENCE": case["reference"], "BASIS_SETS": case["bases"],
             "COORDS": case["coords"], "CHARGE": 0, "MULTIPLICITY": 1, "MAX_SCF_ITERATIONS": 300,
-            **({"EXCITATIONS": case["excitations"]} if case["excitations"] else {})}
+            **({"EXCITATIONS": case["excitations"]} if case["excitations"] else {}),
+            **({"CONSTRAIN_EXCITED": True} if case.get("constrain_excited") else {})}
 
 
 with open(os.path.join(HERE, "golden", "bootstrap.json")) as _fh:
@@ -208,7 +209,8 @@ def test_excitation_keyword_states_match_reference(name, monkeypatch, tmp_path):
     lists, _ = noci.excited_states(mol.NAlphaElectrons, mol.NBetaElectrons, mol.NOrbitals, case["excitations"],
                                    n_core=noci.n_core_orbitals([int(a[1]) for a in case["coords"]]))
     spin_flip = "SF" in case["excitations"]
-    ours = noci.hf_states(eng, lists, spin_flip=spin_flip, reference="UHF")
+    ours = noci.hf_states(eng, lists, spin_flip=spin_flip, reference="UHF",
+                          constrain_excited=bool(case.get("constrain_excited")))
     got = [st["E_hf"] for st in res["states"]]
     assert len(got) == len(case["calls"]) == len(lists)
     assert np.allclose(got, [r.E for r in ours], atol=1e-10)
