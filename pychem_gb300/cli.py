@@ -10,7 +10,9 @@ Keys read:
 
 * ``Method``: HF, MP2, MP2-SCS, MP2-SOS (spin-component scaling of
   ``Methods/mp2.py:97-107``), NOCI (and NOCI-P2 variants, which upstream runs as NOCI).
-* ``Reference``: RHF, UHF, CUHF; ``Constrain_Excited``.
+* ``Reference``: RHF, UHF, CUHF; ``Constrain_Excited``.  As upstream, RHF changes only
+  the printout: closed-shell ground states use the restricted SCF (equal to the
+  unrestricted one there), open shells, excited states and NOCI run unrestricted.
 * ``Coords``, ``Coords_Units`` (ANGSTROM, BOHR), ``Charge``, ``Multiplicity``,
   ``Max_SCF_Iterations``, ``Max_L`` (shells above it dropped).
 * ``Basis_Sets``: each in turn, later ones seeded by orbitals fitted from the previous
@@ -95,6 +97,7 @@ def run_section(name, opts, write, workdir="."):
     eng = _engine(mol)
     res = {"section": name, "basis": basis, "reference": ref, "nbf": mol.NOrbitals}
     write("Section %s: %s/%s %s, %d basis functions" % (name, ref, basis, method, mol.NOrbitals))
+    ref = _effective_reference(mol, opts, ref, method, write)
     if method.startswith("NOCI"):
         out = noci.run(eng, opts.get("EXCITATIONS"), reference=ref,
                        constrain_excited=bool(opts.get("CONSTRAIN_EXCITED", ref == "CUHF")),
@@ -114,12 +117,8 @@ def run_section(name, opts, write, workdir="."):
         _properties(mol, opts, dens, res, write)
         return res
     if ref == "RHF":
-        if mol.NAlphaElectrons != mol.NBetaElectrons:
-            raise ValueError("section %s: RHF needs a closed-shell molecule" % name)
         r = rhf(eng, max_iter=max_iter)
         states = [("ground", r)]
-        if opts.get("EXCITATIONS") is not None:
-            write("Excitations %s: excited states need Reference = UHF or CUHF in this build" % opts["EXCITATIONS"])
     elif opts.get("EXCITATIONS") not in (None, "HOMO-LUMO") or (
             opts.get("EXCITATIONS") == "HOMO-LUMO" and (ref == "CUHF" or opts.get("CONSTRAIN_EXCITED"))):
         # constrained excited states need the occupancy's CUHF spaces (hf_states)
@@ -146,6 +145,20 @@ def run_section(name, opts, write, workdir="."):
         res["states"].append(entry)
     _properties(mol, opts, [scattering.state_densities(st) for _, st in states], res, write)
     return res
+
+
+def _effective_reference(mol, opts, ref, method, write):
+    """Upstream's Reference = RHF changes only the printout (hartree_fock.py:140,150):
+    every state runs through its unrestricted SCF.  The restricted SCF here serves the
+    closed-shell ground state it is equal to; an open-shell molecule, excited states or
+    NOCI under RHF run as UHF."""
+    if ref != "RHF":
+        return ref
+    if (mol.NAlphaElectrons != mol.NBetaElectrons or opts.get("EXCITATIONS") is not None
+            or method.startswith("NOCI")):
+        write("Reference RHF: the states run through the unrestricted SCF, as upstream's do")
+        return "UHF"
+    return ref
 
 
 def _excited_states(mol, eng, opts, ref, max_iter):
@@ -234,9 +247,10 @@ def run_bootstrap(name, opts, write, workdir="."):
     max_iter = int(opts.get("MAX_SCF_ITERATIONS", 128))
     exc = opts.get("EXCITATIONS")
     use_mom = exc is not None
-    if exc not in (None, "HOMO-LUMO") or (exc == "HOMO-LUMO" and ref == "RHF"):
-        write("Excitations %s: not available in this build" % exc)
-    nstates = 2 if (exc == "HOMO-LUMO" and ref != "RHF") else 1
+    if exc not in (None, "HOMO-LUMO"):
+        write("Excitations %s: with several basis sets or MO files only HOMO-LUMO is available in this build"
+              % exc)
+    nstates = 2 if exc == "HOMO-LUMO" else 1
     read = None
     if opts.get("SCF_GUESS") == "READ":
         st, rb = opts.get("MO_READ_STATE"), opts.get("MO_READ_BASIS")
@@ -253,6 +267,7 @@ def run_bootstrap(name, opts, write, workdir="."):
         dev = eng.S.device
         na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
         write("Section %s: %s/%s %s, %d basis functions" % (name, ref, basis, method, mol.NOrbitals))
+        ref = _effective_reference(mol, opts, ref, method, write)
         states = []
         for k in range(nstates):
             C0 = None

@@ -243,3 +243,26 @@ def test_excitation_keyword_states_match_reference(name, monkeypatch, tmp_path):
 
 def basis_name(clean):
     return {"STO3G": "STO-3G", "631G": "6-31G", "CCPVDZ": "cc-pVDZ"}[clean]
+
+
+def test_rhf_sections_that_need_unrestricted_states(monkeypatch, tmp_path):
+    """Upstream's Reference = RHF only changes its printout; its SCF is unrestricted.
+    An RHF section with excited states (H2 HOMO-LUMO) or an open shell (OH) gives the
+    reference's UHF energies (h2_mom_631g, oh_uhf_631g fixtures)."""
+    monkeypatch.setattr(cli, "_engine", OracleEngine)
+    monkeypatch.setattr(cli, "uhf", oracle_uhf)
+    g = np.load(os.path.join(HERE, "golden", "h2_mom_631g.npz"))
+    coords = [[str(a), float(z), *map(float, x)] for a, z, x in zip(g["atoms"], g["charges"], g["coords_bohr"])]
+    opts = {"METHOD": "HF", "REFERENCE": "RHF", "BASIS_SETS": ["6-31G"], "COORDS": coords, "COORDS_UNITS": "BOHR",
+            "EXCITATIONS": "HOMO-LUMO"}
+    lines = []
+    res = cli.run_section("h2", opts, lines.append, str(tmp_path))
+    assert any("unrestricted" in ln for ln in lines)
+    e = [st["E_hf"] for st in res["states"]]
+    assert abs(e[0] - float(g["E_ground"])) < 1e-8 and abs(e[1] - float(g["E_excited"])) < 1e-6
+    o = np.load(os.path.join(HERE, "golden", "oh_uhf_631g.npz"))
+    coords = [[str(a), float(z), *map(float, x)] for a, z, x in zip(o["atoms"], o["charges"], o["coords_bohr"])]
+    opts = {"METHOD": "HF", "REFERENCE": "RHF", "BASIS_SETS": ["6-31G"], "COORDS": coords, "COORDS_UNITS": "BOHR",
+            "MULTIPLICITY": 2}
+    res = cli.run_section("oh", opts, lambda line: None, str(tmp_path))
+    assert abs(res["states"][0]["E_hf"] - float(o["E_scf"])) < 1e-8
