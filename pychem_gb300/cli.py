@@ -14,7 +14,9 @@ Keys read:
   the printout: closed-shell ground states use the restricted SCF (equal to the
   unrestricted one there), open shells, excited states and NOCI run unrestricted.
 * ``Coords``, ``Coords_Units`` (ANGSTROM, BOHR), ``Charge``, ``Multiplicity``,
-  ``Max_SCF_Iterations``, ``Max_L`` (shells above it dropped).
+  ``Max_SCF_Iterations`` (a floor here: at least 128 RHF / 300 UHF iterations with a
+  density criterion, where upstream defaults to 25 and carries on unconverged),
+  ``Max_L`` (shells above it dropped).
 * ``Basis_Sets``: each in turn, later ones seeded by orbitals fitted from the previous
   one (``pychem.py:96-117``, pychem_gb300.basis_fit); NOCI runs in the last one.
 * ``Excitations``: any upstream keyword (``Util/structures.py:393-413``); HOMO-LUMO by
