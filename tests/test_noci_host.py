@@ -357,3 +357,46 @@ def test_ci_matrix_in_chunks_equals_one_pass():
     assert float((H1 - H2).abs().max()) < 1e-12 and float((S1 - S2).abs().max()) < 1e-14
     for x, y in zip(p1, p2):
         assert x.shape == y.shape and float((x.double() - y.double()).abs().max()) < 1e-12
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_ci_matrix_random_determinants(seed):
+    """Random S-orthonormal orbital sets on LiH / 6-31G integrals, some built to share
+    or exclude occupied orbitals (exact zero overlaps in one or both spins, unequal
+    alpha and beta counts): every element against the oracle on the same pairing."""
+    z = load("noci_lih_sfs_631g")
+    S = z["S"]
+    n = S.shape[0]
+    rng = np.random.default_rng(seed)
+    s, U = np.linalg.eigh(S)
+    X = U / np.sqrt(s)                                   # S-orthonormal basis
+
+    def orbitals():
+        Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        return X @ Q
+
+    base = orbitals()
+    swap14 = base.copy()
+    swap14[:, [1, 4]] = swap14[:, [4, 1]]                # one alpha zero against base
+    swap_both = base.copy()
+    swap_both[:, [0, 1, 2, 3]] = swap_both[:, [2, 3, 0, 1]]   # two alpha zeros and a beta zero
+    rnd = orbitals()
+    rnd_swap = rnd.copy()
+    rnd_swap[:, [1, 4]] = rnd_swap[:, [4, 1]]
+    alphas = [base, orbitals(), rnd_swap, swap14, base, swap_both]
+    betas = [base, orbitals(), rnd_swap, swap14, base[:, ::-1].copy(), swap_both]   # 4: a beta zero
+    dets_a = [torch.tensor(c) for c in alphas]
+    dets_b = [torch.tensor(c) for c in betas]
+    na, nb = 2, 1
+    zeng = DenseEngine(z)
+    H, Sm, pairs = noci.noci_matrix(zeng, dets_a, dets_b, na, nb, return_pairs=True)
+    ii, jj, a1, a2, b1, b2 = [t.numpy() for t in pairs]
+    zeros = set()
+    for p in range(len(ii)):
+        zeros.add(oracle.noci_zero_counts(a1[p], a2[p], b1[p], b2[p], S))
+        h, ov = oracle.noci_element_paired(a1[p], a2[p], b1[p], b2[p], S, z["H"], z["eri_dense"], na, nb,
+                                           float(z["E_nuc"]))
+        assert abs(h - H[ii[p], jj[p]].item()) < element_tolerance(a1[p], a2[p], b1[p], b2[p], S, 1e-9)
+        assert abs(ov - Sm[ii[p], jj[p]].item()) < 1e-12
+    assert torch.allclose(H, H.T) and torch.allclose(Sm, Sm.T)
+    assert {(0, 0), (1, 0), (0, 1), (2, 1)} <= zeros      # every element form occurs
