@@ -266,3 +266,40 @@ def test_rhf_sections_that_need_unrestricted_states(monkeypatch, tmp_path):
             "MULTIPLICITY": 2}
     res = cli.run_section("oh", opts, lambda line: None, str(tmp_path))
     assert abs(res["states"][0]["E_hf"] - float(o["E_scf"])) < 1e-8
+
+
+def test_noci_then_scattering_section(monkeypatch, tmp_path):
+    """Method = NOCI with Job_Type = PROPERTY through the runner (make_golden_noci_property.py:
+    H2 / 6-31G, ground and HOMO -> LUMO states): NOCI energies and the scattering table
+    over the NOCI states against the reference, with the oracle standing in for the GPU
+    integrals, UHF, eigensolver and intensity evaluation."""
+    from scipy.linalg import eigh
+    from pychem_gb300 import noci, scattering
+
+    with open(os.path.join(HERE, "golden", "noci_property.json")) as fh:
+        ref = json.load(fh)
+
+    class Engine(OracleEngine):
+        def coulomb_exchange(self, W):
+            E = torch.tensor(self.eri)
+            return torch.einsum("ncd,abcd->nab", W, E), torch.einsum("ncb,abcd->nad", W, E)
+
+    def gen_eigh(H, S):
+        e, v = eigh(H.numpy(), S.numpy())
+        return torch.tensor(e), torch.tensor(v)
+
+    def intensities(mol, grid, densities):
+        b = oracle.Basis([(a[0], a[1], *a[2]) for a in mol.atoms], mol.Basis)
+        return np.array([[oracle.scattering_intensity(np.asarray(a), np.asarray(c), b.eri_dense(scattering=s),
+                                                      mol.NElectrons) for a, c in densities] for s in grid])
+
+    monkeypatch.setattr(cli, "_engine", Engine)
+    monkeypatch.setattr(noci, "uhf", oracle_uhf_states)
+    monkeypatch.setattr(noci, "generalized_eigh", gen_eigh)
+    monkeypatch.setattr(scattering, "intensities", intensities)
+    opts = {"METHOD": "NOCI", "REFERENCE": "UHF", "BASIS_SETS": [ref["basis"]], "COORDS": ref["coords"],
+            "EXCITATIONS": ref["excitations"], "CONSTRAIN_EXCITED": True, "JOB_TYPE": "PROPERTY",
+            "PROPERTY_TYPE": "SCATTERING", "PROPERTY_GRID": ref["grid"]}
+    res = cli.run_section("h2", opts, lambda line: None, str(tmp_path))
+    assert np.abs(np.array(res["noci_energies"]) - ref["noci_energies"]).max() < 1e-6
+    assert np.abs(np.array(res["scattering"]["intensities"]) - np.array(ref["intensities"])).max() < 1e-6
