@@ -303,3 +303,60 @@ def test_noci_then_scattering_section(monkeypatch, tmp_path):
     res = cli.run_section("h2", opts, lambda line: None, str(tmp_path))
     assert np.abs(np.array(res["noci_energies"]) - ref["noci_energies"]).max() < 1e-6
     assert np.abs(np.array(res["scattering"]["intensities"]) - np.array(ref["intensities"])).max() < 1e-6
+
+
+def _cpu_ump2(eng, res, scale=None):
+    """scf.ump2 on CPU: its FP64 transform over the oracle's dense ERI tensor."""
+    from pychem_gb300.scf import ump2
+    return ump2(eng, res, eri=torch.tensor(eng.eri), gemm="fp64", scale=scale)
+
+
+with open(os.path.join(HERE, "golden", "mp2_states.json")) as _fh:
+    MP2_STATES = json.load(_fh)
+
+
+MP2_STATE_ORBITALS = np.load(os.path.join(HERE, "golden", "mp2_states.npz"))
+
+
+def _state_residual(eng, Ca, Cb, occ_a, occ_b, cuhf):
+    """max |F D S - S D F| of a state's orbitals (occupied columns first), with the
+    CUHF constraint of its occupancy when cuhf."""
+    S, H, eri = eng.S.numpy(), eng.H.numpy(), eng.eri
+    na, nb = sum(occ_a), sum(occ_b)
+    Da, Db = Ca[:, :na] @ Ca[:, :na].T, Cb[:, :nb] @ Cb[:, :nb].T
+    J = np.einsum("cd,abcd->ab", Da + Db, eri)
+    Fa = H + J - np.einsum("cb,abcd->ad", Da, eri)
+    Fb = H + J - np.einsum("cb,abcd->ad", Db, eri)
+    if cuhf:
+        tot = [a + b for a, b in zip(occ_a, occ_b)]
+        Fa, Fb = oracle.cuhf_constraint(S, Da, Db, Fa, Fb, na, nb, (tot.count(2), tot.count(1)))
+    return max(float(np.abs(F @ D @ S - S @ D @ F).max()) for F, D in ((Fa, Da), (Fb, Db)))
+
+
+@pytest.mark.parametrize("name", sorted(MP2_STATES))
+def test_mp2_over_excited_states(name, monkeypatch, tmp_path):
+    """Method = MP2 with Excitations = HOMO-LUMO through the runner (UHF: the MOM
+    branch; CUHF: the state loop with the occupancy's constraint spaces), MP2 of every
+    state from its own orbitals and orbital energies, against the reference's printed
+    per-state totals (make_golden_mp2_states.py): 1e-8 / 1e-6 where the reference's
+    state is stationary (orbital gradient below 1e-5), 1e-3 where it stopped short."""
+    from pychem_gb300 import noci
+    case = MP2_STATES[name]
+    monkeypatch.setattr(cli, "_engine", OracleEngine)
+    monkeypatch.setattr(cli, "uhf", oracle_uhf)
+    monkeypatch.setattr(noci, "uhf", oracle_uhf_states)
+    monkeypatch.setattr(cli, "ump2", _cpu_ump2)
+    opts = {"METHOD": "MP2", "REFERENCE": case["reference"], "BASIS_SETS": [case["basis"]],
+            "COORDS": case["coords"], "EXCITATIONS": "HOMO-LUMO", "MAX_SCF_ITERATIONS": 300}
+    res = cli.run_section(name, opts, lambda line: None, str(tmp_path))
+    assert len(res["states"]) == 2
+    mol = Molecule(case["coords"], case["basis"])
+    eng = OracleEngine(mol)
+    lists, _ = noci.excited_states(mol.NAlphaElectrons, mol.NBetaElectrons, mol.NOrbitals, "HOMO-LUMO")
+    for k, st in enumerate(res["states"]):
+        stationary = _state_residual(eng, MP2_STATE_ORBITALS["%s_%d_alpha" % (name, k)],
+                                     MP2_STATE_ORBITALS["%s_%d_beta" % (name, k)], lists[k][0], lists[k][1],
+                                     case["reference"] == "CUHF") < 1e-5
+        e_ref, m_ref = case["E_hf"][k], case["E_mp2_total"][k]
+        assert abs(st["E_hf"] - e_ref) < ((1e-8 if k == 0 else 1e-6) if stationary else 1e-3), (k, st["E_hf"], e_ref)
+        assert abs(st["E_hf"] + st["E_mp2_corr"] - m_ref) < (1e-6 if stationary else 1e-3), (k, m_ref)
