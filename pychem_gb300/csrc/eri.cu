@@ -223,7 +223,7 @@ int pcg_launch_digest(int cls, const DevBasis& b, const DevPairsExt& pr, const i
   case id: k_digest<a, bb, c, d><<<blocks, threads, 0, s>>>(b, pr, tasks, ntask, store, D, G); break;
     PCG_SHAPE_CASES(X)
 #undef X
-    default: return PCG_ERR_ARG;
+    default: pcg_set_error("pcg_digest_class: class id out of range"); return PCG_ERR_ARG;
   }
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;

@@ -10,11 +10,16 @@
 // Every GPU that loads this library holds that array until the process exits.
 //
 // The array is a device symbol: in host code its name is only a stand-in, so the
-// host obtains its device address with cudaGetSymbolAddress, once per device, with
-// that device current, on the first call made on that device.  That first call
-// should therefore come before any stream capture.  Calls share the one array: each
-// call clears it before use, and calls that overlap on the GPU (two streams, or two
-// host threads on one device) race on it and must be serialised by the caller.
+// host obtains its device address with cudaGetSymbolAddress, with the calling device
+// current, on every call (the lookup allocates nothing; repeating it keeps the address
+// right after a cudaDeviceReset reloads the module).  The first call on a device may
+// load the library's device code there, so it should come before any stream capture.
+// Calls share the one array: each call clears the nbf x nbf block it uses, and calls
+// that overlap on the GPU (two streams, or two host threads on one device) race on it
+// and must be serialised by the caller.
+//
+// Every argument is checked before the first CUDA call, so a rejected call launches
+// nothing and leaves both F and the shared array untouched.
 #include <stdio.h>
 
 #include "../../include/pychem_gb300.h"
@@ -24,8 +29,6 @@
 #define PCG_NOALLOC_MAX_NBF 512
 
 static __device__ __align__(256) double g_fock_scratch[PCG_NOALLOC_MAX_NBF * PCG_NOALLOC_MAX_NBF];
-
-static double* g_fock_scratch_addr[64];  // device address per device ordinal
 
 int pcg_launch_fock(int n, const double* H, const double* G, double* F, cudaStream_t s);
 
@@ -71,24 +74,33 @@ extern "C" int pcg_fock_build_noalloc(const pcg_basis_t* basis, const pcg_pairs_
     pcg_set_error(msg);
     return PCG_ERR_CAPACITY;
   }
-  int dev = 0;
-  PCG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) { pcg_set_error("pcg_fock_build_noalloc: device ordinal out of range"); return PCG_ERR_ARG; }
-  if (!g_fock_scratch_addr[dev]) {
-    double* p = nullptr;
-    PCG_CUDA(cudaGetSymbolAddress((void**)&p, g_fock_scratch));
-    g_fock_scratch_addr[dev] = p;
+  // the accumulator is addressed with row stride nbf: any other matrix layout would
+  // index past the cleared block (and, for ld > 512, past the array)
+  if (basis->ld > 0 && basis->ld != n) {
+    pcg_set_error("pcg_fock_build_noalloc: basis->ld must be 0 or nbf (one molecule, nbf x nbf matrices)");
+    return PCG_ERR_ARG;
   }
-  double* G = g_fock_scratch_addr[dev];
-  cudaStream_t s = (cudaStream_t)stream;
-  PCG_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * (size_t)n * n, s));
-  const DevBasis b = basis_of(basis);
-  const DevPairsExt pr = pairs_of(pairs);
   for (int k = 0; k < nclass; ++k) {
-    if (cls[k] < 0 || cls[k] > 20 || ntask[k] < 0) {
-      pcg_set_error("pcg_fock_build_noalloc: bad class entry");
+    if (cls[k] < 0 || cls[k] > 20 || ntask[k] < 0 || (ntask[k] > 0 && (!tasks[k] || !stores[k]))) {
+      char msg[120];
+      snprintf(msg, sizeof(msg), "pcg_fock_build_noalloc: bad class entry %d", k);
+      pcg_set_error(msg);
       return PCG_ERR_ARG;
     }
+  }
+  int dev = 0;
+  PCG_CUDA(cudaGetDevice(&dev));
+  double* G = nullptr;
+  PCG_CUDA(cudaGetSymbolAddress((void**)&G, g_fock_scratch));
+  cudaStream_t s = (cudaStream_t)stream;
+  PCG_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * (size_t)n * n, s));
+  DevBasis b = basis_of(basis);
+  b.ld = n;
+  DevPairsExt pr = pairs_of(pairs);
+  // the digestion then reads AO offsets from the shell tables, whose block offset is 0
+  // without sh_blk, instead of the optional per-pair table with its own offsets
+  pr.p.ao4 = nullptr;
+  for (int k = 0; k < nclass; ++k) {
     int rc = pcg_launch_digest(cls[k], b, pr, (const int2*)tasks[k], ntask[k], stores[k], D, G, s);
     if (rc) return rc;
   }

@@ -31,4 +31,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYCHEM_REFERENCE")
+    if not src:
+        sys.exit("usage: extract_basis.py <reference tree>  (or set PYCHEM_REFERENCE)")
+    main(src)

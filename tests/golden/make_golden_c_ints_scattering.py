@@ -1,7 +1,7 @@
 """Recorded ``_c_ints`` calls of the upstream scattering-integral path.
 
-Run once in a container that holds the reference tree (``PYCHEM_REFERENCE``,
-default ``/root/reference``):
+Run once where the reference tree is present, its path in the environment
+variable ``PYCHEM_REFERENCE`` (required):
 
     python tests/golden/make_golden_c_ints_scattering.py
 

@@ -1,7 +1,7 @@
 """State and spin-flip determinant lists from the upstream pychem reference.
 
-Run once in a container that holds the reference tree (``PYCHEM_REFERENCE``,
-default ``/root/reference``):
+Run once where the reference tree is present, its path in the environment
+variable ``PYCHEM_REFERENCE`` (required):
 
     python tests/golden/make_golden_excitations.py
 

@@ -1,7 +1,7 @@
 """NOCI followed by scattering properties, from the upstream pychem reference.
 
-Run once in a container that holds the reference tree (``PYCHEM_REFERENCE``,
-default ``/root/reference``):
+Run once where the reference tree is present, its path in the environment
+variable ``PYCHEM_REFERENCE`` (required):
 
     python tests/golden/make_golden_noci_property.py
 

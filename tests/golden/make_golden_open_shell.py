@@ -1,7 +1,7 @@
 """Open-shell golden fixtures (UHF, CUHF, UMP2) from the upstream pychem reference.
 
-Run once in a container that holds the reference tree (``PYCHEM_REFERENCE``,
-default ``/root/reference``):
+Run once where the reference tree is present, its path in the environment
+variable ``PYCHEM_REFERENCE`` (required):
 
     python tests/golden/make_golden_open_shell.py
 

@@ -28,7 +28,7 @@ import tempfile
 
 import numpy as np
 
-REFERENCE = os.environ.get("PYCHEM_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("PYCHEM_REFERENCE")  # path of the reference tree; no default
 
 # Boys table layout fixed by interpolation_table.h:4-14
 N_POINTS = 7750
@@ -142,8 +142,8 @@ _C_SOURCES = [
 
 def prepare(workdir=None):
     """Patched, built copy of the reference; returns its root directory."""
-    if not os.path.isdir(REFERENCE):
-        raise RuntimeError("reference tree not found at %s" % REFERENCE)
+    if not REFERENCE or not os.path.isdir(REFERENCE):
+        raise RuntimeError("set PYCHEM_REFERENCE to the path of the reference tree (now %r)" % REFERENCE)
     root = os.path.join(workdir or tempfile.mkdtemp(prefix="pychem_ref_"), "ref")
     shutil.copytree(REFERENCE, root, copy_function=shutil.copyfile)
     for dirpath, _, files in os.walk(root):

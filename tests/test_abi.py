@@ -50,3 +50,26 @@ def test_generated_header_is_current():
     import sys
     r = subprocess.run([sys.executable, os.path.join(REPO, "pychem_gb300", "csrc", "gen_eri.py"), "--check"])
     assert r.returncode == 0
+
+
+def test_noalloc_fock_rejects_bad_layout_before_any_cuda_call(lib):
+    # pcg_fock_build_noalloc checks its arguments before its first CUDA call, so these
+    # calls run without a GPU: a row stride other than nbf would index past the
+    # cleared part of the static accumulator, and a bad class entry must be refused
+    # before anything is queued.
+    import ctypes
+    from pychem_gb300._lib import BasisT, PairsT
+    fake = ctypes.c_void_p(16)          # never dereferenced: every call below is rejected
+    b, p = BasisT(), PairsT()
+    b.nbf, b.ld = 100, 101
+    assert lib.pcg_fock_build_noalloc(ctypes.byref(b), ctypes.byref(p), 0, None, None, None, None,
+                                      fake, fake, fake, None) == 2
+    assert b"ld must be 0 or nbf" in lib.pcg_last_error()
+    b.ld = 100
+    cls = (ctypes.c_int * 2)(0, 21)
+    ntask = (ctypes.c_int * 2)(1, 1)
+    ptrs = (ctypes.c_void_p * 2)(16, 16)
+    assert lib.pcg_fock_build_noalloc(ctypes.byref(b), ctypes.byref(p), 2, ctypes.cast(cls, ctypes.c_void_p),
+                                      ctypes.cast(ptrs, ctypes.c_void_p), ctypes.cast(ntask, ctypes.c_void_p),
+                                      ctypes.cast(ptrs, ctypes.c_void_p), fake, fake, fake, None) == 2
+    assert b"bad class entry 1" in lib.pcg_last_error()

@@ -25,9 +25,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import refrun  # noqa: E402
 
-TESTS = os.path.join(refrun.REFERENCE, "Tests")
+TESTS = os.path.join(refrun.REFERENCE, "Tests") if refrun.REFERENCE else ""
 pytestmark = pytest.mark.skipif(not os.path.isfile(os.path.join(TESTS, "integration_tests.py")),
-                                reason="reference tree not present")
+                                reason="reference tree not present (set PYCHEM_REFERENCE)")
 
 
 def expectations():

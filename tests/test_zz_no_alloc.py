@@ -52,6 +52,27 @@ def test_noalloc_fock_matches_allocating_path(golden_dir):
         np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10, err_msg="call %d" % call)
 
 
+def test_noalloc_fock_near_the_size_limit():
+    """21 waters in cc-pVDZ: 504 basis functions, s/p/d shells, close to the 512 limit
+    of the static accumulator, so nearly the whole array is cleared and indexed."""
+    from pychem_gb300 import workloads as W
+    from pychem_gb300.engine import GpuEngine
+    from pychem_gb300.molecule import Molecule
+    mol = Molecule(W.water_cluster(7, 3, 1, seed=5), "cc-pVDZ")
+    assert 480 <= mol.NOrbitals <= 512
+    from pychem_gb300.guess import sad_density
+    eng = GpuEngine(mol).prepare()
+    rng = np.random.default_rng(12)
+    D0 = sad_density(mol, device="cuda")
+    for call in range(2):
+        # a physical (SAD) density, then the same with a small symmetric perturbation
+        M = rng.normal(size=(eng.nbf, eng.nbf)) * 1e-3 * call
+        D = D0 + torch.tensor(M + M.T, device="cuda")
+        ref = eng.fock(D).cpu().numpy()
+        got = _noalloc_fock(eng, D).cpu().numpy()
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10, err_msg="call %d" % call)
+
+
 def test_noalloc_rejects_too_many_basis_functions():
     from pychem_gb300 import _lib
     from pychem_gb300._lib import BasisT, PairsT
