@@ -42,6 +42,16 @@ def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def oracle_energies():
+    """Oracle energies of the benchmark configurations (tests/golden/configs.json,
+    made by tests/golden/make_golden_configs.py); {} when absent."""
+    try:
+        with open(os.path.join(REPO, "tests", "golden", "configs.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
 def load_peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
@@ -356,6 +366,11 @@ def alkane_leg(torch, args):
                      "iterations": r.iterations, "quartets_fp32": eng.stats["quartets_fp32"],
                      "quartets_fp64": eng.stats["quartets_fp64"]}
     out["dE_mixed_vs_fp64"] = out["mixed"]["E_rhf"] - out["fp64"]["E_rhf"]
+    ref = oracle_energies().get("c3_c12h26_ccpvdz")
+    if ref:
+        out["E_rhf_oracle"] = ref["E_rhf"]
+        out["dE_fp64_vs_oracle"] = out["fp64"]["E_rhf"] - ref["E_rhf"]
+        out["dE_mixed_vs_oracle"] = out["mixed"]["E_rhf"] - ref["E_rhf"]
     out["eri_speedup_mixed"] = out["fp64"]["eri_s"] / out["mixed"]["eri_s"]
     return out
 
@@ -617,6 +632,12 @@ def gpu_arm(args):
                "eri_quartets_per_s": rate}
 
     achieved = eri_flops / t_eri / 1e12
+    ref = oracle_energies().get("c2_water16_631g", {})
+    vs_oracle = {"E_rhf_oracle": ref.get("E_rhf"), "E_mp2_corr_oracle": ref.get("E_mp2_corr"),
+                 "dE_rhf": r.E - ref["E_rhf"] if ref else None,
+                 "dE_mp2_corr": e2 - ref["E_mp2_corr"] if ref else None,
+                 "dE_rhf_mixed": rm.E - ref["E_rhf"] if ref else None,
+                 "dE_mp2_corr_mixed": e2m - ref["E_mp2_corr"] if ref else None}
     line = {
         "metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
@@ -624,7 +645,7 @@ def gpu_arm(args):
         "config": {"workload": WORKLOAD, "basis": "6-31G", "nbf": n, "n_occ": o, "seed": SEED,
                    "screening": "Schwarz 1e-8", "scf": "|dE|<1e-10 and D-RMS<1e-8, DIIS(10)",
                    "l2": "256 MiB buffer written between steps", "parallelism": "replicas" if world > 1 else "single"},
-        "E_rhf": r.E, "E_mp2_total": r.E + e2, "scf_iterations": r.iterations,
+        "E_rhf": r.E, "E_mp2_total": r.E + e2, "scf_iterations": r.iterations, "vs_oracle": vs_oracle,
         "eri_shell_quartets": quartets,
         "eri_quartets_per_s": quartets / t_eri,
         "fock_builds_per_s": 1.0 / t_fock,

@@ -198,7 +198,7 @@ static void nuclear_prim(int la, int lb, const double *A, const double *B, doubl
     double F[OR_MAXLT + 2];
     oracle_boys(L, zeta * r2, F);
     /* table V[ga][gb][m] */
-    static double V[35][35][OR_MAXLT + 2];
+    static __thread double V[35][35][OR_MAXLT + 2];
     int na = cart_offset(la + 1), nb = cart_offset(lb + 1);
     double pre = -Z * 2.0 * sqrt(zeta / M_PI) * U; /* = -Z 2pi/zeta K_AB */
     for (int m = 0; m <= L; ++m) V[0][0][m] = pre * F[m];
@@ -371,10 +371,10 @@ static void eri_cart(const or_shell *sa, const or_shell *sb, const or_shell *sc,
     const double *A = sa->center, *B = sb->center, *C = sc->center, *D = sd->center;
     double AB2 = 0.0, CD2 = 0.0;
     for (int i = 0; i < 3; ++i) { AB2 += (A[i] - B[i]) * (A[i] - B[i]); CD2 += (C[i] - D[i]) * (C[i] - D[i]); }
-    static double V[NE_MAX][NE_MAX][OR_MAXLT + 1];
-    static double acc[NE_MAX][NE_MAX];
+    static __thread double V[NE_MAX][NE_MAX][OR_MAXLT + 1];
+    static __thread double acc[NE_MAX][NE_MAX];
     memset(acc, 0, sizeof(acc));
-    static int comp[NE_MAX][3];
+    static __thread int comp[NE_MAX][3];
     for (int l = 0; l <= 4; ++l) {
         int cc[15][3]; list_cart(l, cc);
         for (int k = 0; k < ncart(l); ++k) memcpy(comp[cart_offset(l) + k], cc[k], sizeof(int) * 3);
@@ -470,9 +470,9 @@ static void eri_cart(const or_shell *sa, const or_shell *sb, const or_shell *sc,
         }
     }
     /* bra HRR: (a,b+1i| = (a+1i,b| + AB_i (a,b|  on contracted integrals, all ket f */
-    static double H1[NE_MAX][15][NE_MAX]; /* [a global][b cart idx within lb-level][f] */
+    static __thread double H1[NE_MAX][15][NE_MAX]; /* [a global][b cart idx within lb-level][f] */
     /* store by (a global, b global) using a small map: b global index <= cart_offset(lb+1) */
-    static double HB[NE_MAX][10][NE_MAX];
+    static __thread double HB[NE_MAX][10][NE_MAX];
     int nbg = cart_offset(lb + 1);
     for (int g = 0; g < NE; ++g) for (int h = 0; h < NF; ++h) HB[g][0][h] = acc[g][h];
     double AB[3] = {A[0] - B[0], A[1] - B[1], A[2] - B[2]};
@@ -495,7 +495,7 @@ static void eri_cart(const or_shell *sa, const or_shell *sb, const or_shell *sc,
     /* ket HRR on the (la, lb) bra block */
     int nca = ncart(la), ncb = ncart(lb), ncc = ncart(lc), ncd = ncart(ld);
     int ndg = cart_offset(ld + 1);
-    static double HK[15 * 15][NE_MAX][10];
+    static __thread double HK[15 * 15][NE_MAX][10];
     for (int ka = 0; ka < nca; ++ka)
         for (int kb = 0; kb < ncb; ++kb) {
             int ga = cart_offset(la) + ka, gb = cart_offset(lb) + kb, r = ka * ncb + kb;
@@ -546,3 +546,206 @@ double oracle_eri_list(const or_shell *shells, int nq, const int *quads)
 }
 
 int oracle_sizeof_shell(void) { return (int)sizeof(or_shell); }
+
+/* ----------------------------------------------------------------------------------
+ * Packed store: the screened unique shell quartets of a molecule and their blocks,
+ * for systems whose dense N^4 tensor does not fit in host memory (upstream keeps the
+ * dense tensor, Methods/hartree_fock.py:241-325 into Util/structures.py:506).  Each
+ * quartet (a b | c d) lists shells a <= b, c <= d, with the pair (c, d) not after
+ * (a, b) in pair order; its block is the spherical [na][nb][nc][nd] of
+ * oracle_eri_quartet at offset boff[q].  Threads take quartets (or occupied orbitals)
+ * in turn; nothing is shared between them but read-only inputs.
+ * ---------------------------------------------------------------------------------- */
+#include <pthread.h>
+
+typedef struct {
+    const or_shell *sh;
+    const int *quads;
+    const long long *boff;
+    double *blocks;
+    int nq, t, nt;
+} or_eri_job;
+
+static void *or_eri_worker(void *arg)
+{
+    or_eri_job *j = (or_eri_job *)arg;
+    for (int q = j->t; q < j->nq; q += j->nt) {
+        const int *x = j->quads + 4 * q;
+        oracle_eri_quartet(&j->sh[x[0]], &j->sh[x[1]], &j->sh[x[2]], &j->sh[x[3]], j->blocks + j->boff[q]);
+    }
+    return NULL;
+}
+
+/* Blocks of nq quartets into blocks[boff[q] ...], on nthreads threads. */
+int oracle_eri_blocks(const or_shell *shells, int nq, const int *quads, const long long *boff, double *blocks,
+                      int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    or_eri_job jobs[256];
+    for (int t = 0; t < nthreads; ++t) {
+        jobs[t] = (or_eri_job){shells, quads, boff, blocks, nq, t, nthreads};
+        if (pthread_create(&th[t], NULL, or_eri_worker, &jobs[t]) != 0) return -1;
+    }
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    return 0;
+}
+
+/* The distinct index permutations (p q | r s) of one unique element: the 8 images of
+ * the permutational symmetry with repeats removed.  Returns their count. */
+static int or_images(int m, int n, int l, int s, int img[8][4])
+{
+    const int cand[8][4] = {{m, n, l, s}, {n, m, l, s}, {m, n, s, l}, {n, m, s, l},
+                            {l, s, m, n}, {s, l, m, n}, {l, s, n, m}, {s, l, n, m}};
+    int k = 0;
+    for (int c = 0; c < 8; ++c) {
+        int dup = 0;
+        for (int e = 0; e < k && !dup; ++e)
+            dup = img[e][0] == cand[c][0] && img[e][1] == cand[c][1] && img[e][2] == cand[c][2] &&
+                  img[e][3] == cand[c][3];
+        if (!dup) {
+            for (int i = 0; i < 4; ++i) img[k][i] = cand[c][i];
+            ++k;
+        }
+    }
+    return k;
+}
+
+/* Visit every unique element of quartet q once: within a block whose two shells of a
+ * pair coincide only one of (mu nu) / (nu mu) is unique, and for a quartet whose bra
+ * and ket pairs coincide only one of (mu nu | lam sig) / (lam sig | mu nu). */
+#define OR_FOR_UNIQUE(sh, ao, x, blk, ...)                                                               \
+    do {                                                                                                 \
+        const int a_ = (x)[0], b_ = (x)[1], c_ = (x)[2], d_ = (x)[3];                                    \
+        const int na_ = 2 * (sh)[a_].l + 1, nb_ = 2 * (sh)[b_].l + 1, nc_ = 2 * (sh)[c_].l + 1,          \
+                  nd_ = 2 * (sh)[d_].l + 1;                                                              \
+        const int same_bra_ket_ = a_ == c_ && b_ == d_;                                                  \
+        for (int i_ = 0; i_ < na_; ++i_)                                                                 \
+            for (int j_ = 0; j_ < nb_; ++j_) {                                                           \
+                if (a_ == b_ && j_ > i_) continue;                                                       \
+                for (int k_ = 0; k_ < nc_; ++k_)                                                         \
+                    for (int l_ = 0; l_ < nd_; ++l_) {                                                   \
+                        if (c_ == d_ && l_ > k_) continue;                                               \
+                        if (same_bra_ket_ && (k_ * nd_ + l_) > (i_ * nb_ + j_)) continue;                \
+                        const double v = (blk)[((i_ * nb_ + j_) * nc_ + k_) * nd_ + l_];                 \
+                        const int mu = (ao)[a_] + i_, nu = (ao)[b_] + j_, la = (ao)[c_] + k_,            \
+                                  si = (ao)[d_] + l_;                                                    \
+                        __VA_ARGS__                                                                      \
+                    }                                                                                    \
+            }                                                                                            \
+    } while (0)
+
+typedef struct {
+    const or_shell *sh;
+    const int *ao, *quads;
+    const long long *boff;
+    const double *blocks, *Dj, *Dk;
+    double *J, *K;
+    int nq, n, t, nt;
+} or_jk_job;
+
+static void *or_jk_worker(void *arg)
+{
+    or_jk_job *j = (or_jk_job *)arg;
+    const int n = j->n;
+    for (int q = j->t; q < j->nq; q += j->nt) {
+        const int *x = j->quads + 4 * q;
+        const double *blk = j->blocks + j->boff[q];
+        OR_FOR_UNIQUE(j->sh, j->ao, x, blk, {
+            int img[8][4];
+            const int ni = or_images(mu, nu, la, si, img);
+            for (int e = 0; e < ni; ++e) {
+                const int p = img[e][0], qq = img[e][1], r = img[e][2], s = img[e][3];
+                j->J[p * n + qq] += j->Dj[r * n + s] * v;  /* J_pq = sum_rs (pq|rs) Dj_rs */
+                j->K[p * n + s] += j->Dk[r * n + qq] * v;  /* K_ps = sum_qr (pq|rs) Dk_rq */
+            }
+        });
+    }
+    return NULL;
+}
+
+/* J = einsum('cd,abcd->ab', Dj, ERI) and K = einsum('cb,abcd->ad', Dk, ERI) over the
+ * packed store (Methods/hartree_fock.py:345-347); ao[shell] = first AO of the shell,
+ * J and K (n x n) are overwritten. */
+int oracle_jk_packed(const or_shell *shells, const int *ao, int nq, const int *quads, const long long *boff,
+                     const double *blocks, int n, const double *Dj, const double *Dk, double *J, double *K,
+                     int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    const size_t nn = (size_t)n * n;
+    double *buf = (double *)calloc((size_t)nthreads * 2 * nn, sizeof(double));
+    if (!buf) return -1;
+    pthread_t th[256];
+    or_jk_job jobs[256];
+    for (int t = 0; t < nthreads; ++t) {
+        jobs[t] = (or_jk_job){shells, ao, quads, boff, blocks, Dj, Dk, buf + 2 * t * nn, buf + (2 * t + 1) * nn,
+                              nq, n, t, nthreads};
+        if (pthread_create(&th[t], NULL, or_jk_worker, &jobs[t]) != 0) { free(buf); return -1; }
+    }
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    for (size_t e = 0; e < nn; ++e) {
+        double sj = 0.0, sk = 0.0;
+        for (int t = 0; t < nthreads; ++t) { sj += buf[2 * t * nn + e]; sk += buf[(2 * t + 1) * nn + e]; }
+        J[e] = sj;
+        K[e] = sk;
+    }
+    free(buf);
+    return 0;
+}
+
+typedef struct {
+    const or_shell *sh;
+    const int *ao, *quads;
+    const long long *boff;
+    const double *blocks, *C;
+    double *T;
+    int nq, n, o, i0, i1;
+} or_q1_job;
+
+static void *or_q1_worker(void *arg)
+{
+    or_q1_job *j = (or_q1_job *)arg;
+    const int n = j->n, o = j->o;
+    const long long np = (long long)n * (n + 1) / 2;
+    for (int q = 0; q < j->nq; ++q) {
+        const int *x = j->quads + 4 * q;
+        const double *blk = j->blocks + j->boff[q];
+        OR_FOR_UNIQUE(j->sh, j->ao, x, blk, {
+            int img[8][4];
+            const int ni = or_images(mu, nu, la, si, img);
+            for (int e = 0; e < ni; ++e) {
+                const int p = img[e][0], qq = img[e][1], r = img[e][2], s = img[e][3];
+                if (r < s) continue;  /* the (s r) image carries the same pair */
+                const long long rs = (long long)r * (r + 1) / 2 + s;
+                for (int i = j->i0; i < j->i1; ++i)
+                    j->T[((long long)i * n + qq) * np + rs] += j->C[(long long)p * o + i] * v;
+            }
+        });
+    }
+    return NULL;
+}
+
+/* First quarter of the MP2 AO->MO transform (Methods/mp2.py:43-69) over the packed
+ * store: T[i][nu][rs] = sum_mu C[mu][i] (mu nu | r s) for the o columns of C (n x o,
+ * row-major) and the lower-triangle pair index rs = r(r+1)/2 + s, r >= s.  T
+ * (o x n x n(n+1)/2) is accumulated into (zero it first).  Threads split the
+ * occupied index, so each reads the whole store. */
+int oracle_mp2_first_quarter(const or_shell *shells, const int *ao, int nq, const int *quads,
+                             const long long *boff, const double *blocks, int n, int o, const double *C, double *T,
+                             int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > o) nthreads = o;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    or_q1_job jobs[256];
+    for (int t = 0; t < nthreads; ++t) {
+        const int i0 = (int)((long long)o * t / nthreads), i1 = (int)((long long)o * (t + 1) / nthreads);
+        jobs[t] = (or_q1_job){shells, ao, quads, boff, blocks, C, T, nq, n, o, i0, i1};
+        if (pthread_create(&th[t], NULL, or_q1_worker, &jobs[t]) != 0) return -1;
+    }
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    return 0;
+}

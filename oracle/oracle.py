@@ -59,7 +59,7 @@ def build(force=False):
     """Compile the C oracle (gcc, no GPU)."""
     src = os.path.join(HERE, "hgp_oracle.c")
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
-        subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-o", LIB_PATH, src, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-pthread", "-o", LIB_PATH, src, "-lm"])
     return LIB_PATH
 
 
@@ -80,6 +80,12 @@ def lib():
         L.oracle_boys.argtypes = [ctypes.c_int, ctypes.c_double, P(ctypes.c_double)]
         L.oracle_set_operator.argtypes = [ctypes.c_int, ctypes.c_double]
         L.oracle_sph_bessel.argtypes = [ctypes.c_int, ctypes.c_double, P(ctypes.c_double)]
+        vp = ctypes.c_void_p
+        L.oracle_eri_blocks.argtypes = [P(OrShell), ctypes.c_int, vp, vp, vp, ctypes.c_int]
+        L.oracle_jk_packed.argtypes = [P(OrShell), vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, vp, vp, vp, vp,
+                                       ctypes.c_int]
+        L.oracle_mp2_first_quarter.argtypes = [P(OrShell), vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                               vp, vp, ctypes.c_int]
         assert L.oracle_sizeof_shell() == ctypes.sizeof(OrShell)
         _lib = L
     return _lib
@@ -198,6 +204,21 @@ class Basis:
                     out.append((a, b, c, d))
         return out
 
+    def quartet_array(self, Q=None):
+        """quartets() as an int32 array (nq, 4), listed in the same order without a
+        Python loop over quartets (for molecules with millions of them)."""
+        if Q is None:
+            Q = self.schwarz()
+        ia, ib = np.triu_indices(self.nshell)
+        q = Q[ia, ib]
+        rows = []
+        for i in range(len(ia)):
+            js = np.nonzero(q[: i + 1] * q[i] > INTEGRAL_THRESHOLD)[0]
+            if len(js) == 0 or js[-1] != i:
+                js = np.append(js, i)
+            rows.append(np.stack([np.full(len(js), ia[i]), np.full(len(js), ib[i]), ia[js], ib[js]], axis=1))
+        return np.ascontiguousarray(np.concatenate(rows).astype(np.int32))
+
     def eri_dense(self, scattering=None):
         """Dense ERI tensor over the screened quartets (hartree_fock.py:241-327); with
         scattering = S the operator is j0(S r12) (the integrals of
@@ -224,6 +245,78 @@ class Basis:
             eri[C, D, B, A] = blk.transpose(2, 3, 1, 0)
             eri[D, C, B, A] = blk.transpose(3, 2, 1, 0)
         return eri
+
+
+class PackedStore:
+    """The screened unique shell quartets of a Basis and their blocks, computed by the
+    C oracle on several threads, for molecules whose dense N^4 tensor does not fit in
+    host memory.  jk() and mp2_first_quarter() contract it without expanding it."""
+
+    def __init__(self, basis, nthreads=None, Q=None):
+        self.basis = basis
+        self.nthreads = nthreads or os.cpu_count() or 1
+        self.quads = basis.quartet_array(Q)
+        ls = np.array([s[0] for s in basis.shells])
+        dims = 2 * ls + 1
+        size = dims[self.quads[:, 0]] * dims[self.quads[:, 1]] * dims[self.quads[:, 2]] * dims[self.quads[:, 3]]
+        self.boff = np.ascontiguousarray(np.concatenate([[0], np.cumsum(size)[:-1]]).astype(np.int64))
+        self.blocks = np.empty(int(size.sum()))
+        self.ao = np.ascontiguousarray(basis.offsets, dtype=np.int32)
+        self.n = basis.nbf
+        rc = lib().oracle_eri_blocks(basis.c, len(self.quads), self.quads.ctypes.data, self.boff.ctypes.data,
+                                     self.blocks.ctypes.data, self.nthreads)
+        if rc != 0:
+            raise RuntimeError("oracle_eri_blocks failed")
+
+    @property
+    def nquartets(self):
+        return len(self.quads)
+
+    def jk(self, Dj, Dk):
+        """J = einsum('cd,abcd->ab', Dj, ERI), K = einsum('cb,abcd->ad', Dk, ERI)."""
+        n = self.n
+        Dj, Dk = np.ascontiguousarray(Dj, dtype=float), np.ascontiguousarray(Dk, dtype=float)
+        J, K = np.empty((n, n)), np.empty((n, n))
+        rc = lib().oracle_jk_packed(self.basis.c, self.ao.ctypes.data, len(self.quads), self.quads.ctypes.data,
+                                    self.boff.ctypes.data, self.blocks.ctypes.data, n, Dj.ctypes.data,
+                                    Dk.ctypes.data, J.ctypes.data, K.ctypes.data, self.nthreads)
+        if rc != 0:
+            raise RuntimeError("oracle_jk_packed failed")
+        return J, K
+
+    def mp2_first_quarter(self, Co):
+        """T[i][nu][rs] = sum_mu Co[mu][i] (mu nu | r s), rs = r(r+1)/2 + s, r >= s."""
+        n, o = Co.shape
+        Co = np.ascontiguousarray(Co, dtype=float)
+        T = np.zeros((o, n, n * (n + 1) // 2))
+        rc = lib().oracle_mp2_first_quarter(self.basis.c, self.ao.ctypes.data, len(self.quads),
+                                            self.quads.ctypes.data, self.boff.ctypes.data, self.blocks.ctypes.data,
+                                            n, o, Co.ctypes.data, T.ctypes.data, self.nthreads)
+        if rc != 0:
+            raise RuntimeError("oracle_mp2_first_quarter failed")
+        return T
+
+
+def rmp2_packed(C, eps, store, nocc):
+    """rmp2() over a PackedStore: first quarter transform from the store (C), the
+    other three by dense products one occupied orbital at a time, so that neither the
+    dense AO tensor nor a full N^3 o intermediate is held."""
+    n = C.shape[0]
+    Co, Cv = C[:, :nocc], C[:, nocc:]
+    v = Cv.shape[1]
+    T1 = store.mp2_first_quarter(Co)                     # (i, nu, rs)
+    r, s_ = np.tril_indices(n)
+    ovov = np.empty((nocc, v, nocc, v))
+    M = np.zeros((v, n, n))
+    for i in range(nocc):
+        T2 = Cv.T @ T1[i]                                # (a, rs)
+        M[:, r, s_] = T2
+        M[:, s_, r] = T2
+        ovov[i] = np.einsum("alk,lj,kb->ajb", M, Co, Cv, optimize=True)
+    del T1
+    eo, ev = eps[:nocc], eps[nocc:]
+    denom = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
+    return float(np.sum(ovov * (2.0 * ovov - ovov.transpose(0, 3, 2, 1)) / denom))
 
 
 def pack8(eri):
@@ -259,8 +352,9 @@ def orthogonaliser(S):
 
 
 def rhf(S, H, eri, nocc, e_nuc, mode="consistent", max_iter=200, e_tol=1e-10, d_tol=1e-8,
-        diis_size=None, D0=None):
-    """Returns dict(E, C, eps, D, iterations, converged)."""
+        diis_size=None, D0=None, store=None):
+    """Returns dict(E, C, eps, D, iterations, converged).  With a PackedStore in
+    ``store`` (and eri None) the Coulomb and exchange matrices come from it."""
     X = orthogonaliser(S)
     Xt = X.T
 
@@ -276,6 +370,9 @@ def rhf(S, H, eri, nocc, e_nuc, mode="consistent", max_iter=200, e_tol=1e-10, d_
     F = H.copy()
 
     def fock(D):
+        if store is not None:
+            J, K = store.jk(2.0 * D, D)
+            return H + J - K
         J = np.einsum("cd,abcd->ab", 2.0 * D, eri, optimize=True)
         K = np.einsum("cb,abcd->ad", D, eri, optimize=True)
         return H + J - K
