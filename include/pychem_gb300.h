@@ -268,6 +268,21 @@ size_t pcg_ozaki_workspace(const pcg_gemm_desc_t *desc, int nslice);
 int pcg_ozaki_gemm(const pcg_gemm_desc_t *desc, const double *A, const double *B, double *C, int nslice,
                    int accumulate, void *workspace, size_t ws_bytes, void *stream);
 
+/* FP64-accurate GEMM with every Ozaki level in one tcgen05 tensor-core kernel (no
+ * upstream counterpart; it carries the AO->MO transform of Methods/mp2.py:43-69 and
+ * the density C_occ C_occ^T of Methods/hartree_fock.py:179-184):
+ *   C[m*sCm + n*sCn] (+)= sum_k X[m*ldx + k] * Y[k*sYk + n*sYn],  0 <= m < M, n < N.
+ * X (rows contiguous along k, ldx >= K) is split into nslice 7-bit BF16 digit slices
+ * inside the kernel; Y is split once into the workspace.  nslice 6 or 7;
+ * K * (nslice + 2) < 4096; workspace: pcg_ozaki_tc_workspace(N, K, nslice) bytes,
+ * 256-byte aligned, caller-owned device memory.  pcg_ozaki_tc_status: the error flag
+ * a kernel sets when it gives up on a bounded wait (0 = none), read synchronously. */
+size_t pcg_ozaki_tc_workspace(int N, int K, int nslice);
+int pcg_ozaki_gemm_tc(int M, int N, int K, const double *X, long long ldx, const double *Y, long long sYk,
+                      long long sYn, double *C, long long sCm, long long sCn, int nslice, int accumulate,
+                      void *workspace, size_t ws_bytes, void *stream);
+int pcg_ozaki_tc_status(const void *workspace, void *stream);
+
 /* Batched symmetric eigensolver (no upstream counterpart; replaces the LAPACK eigh of
  * Methods/hartree_fock.py:172-175,226): parallel cyclic Jacobi, one CTA per matrix.
  * A: batch x n x n FP64 (read only); w: batch x n eigenvalues (unsorted, matching the

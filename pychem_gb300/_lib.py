@@ -93,6 +93,10 @@ _SIGS = {
                         c_void_p],
     "pcg_ozaki_gemm": [ctypes.c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, ctypes.c_size_t,
                        c_void_p],
+    "pcg_ozaki_tc_workspace": [c_int, c_int, c_int],
+    "pcg_ozaki_gemm_tc": [c_int, c_int, c_int, c_void_p, c_longlong, c_void_p, c_longlong, c_longlong, c_void_p,
+                          c_longlong, c_longlong, c_int, c_int, c_void_p, ctypes.c_size_t, c_void_p],
+    "pcg_ozaki_tc_status": [c_void_p, c_void_p],
     "pcg_fock_build_noalloc": [ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_int, c_void_p, c_void_p, c_void_p,
                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
 }
@@ -105,7 +109,10 @@ LAUNCHERS = {"pcg_pair_data", "pcg_pair_data_f32", "pcg_pair_ao", "pcg_one_elect
              "pcg_one_electron_fundamentals", "pcg_one_electron_vrr", "pcg_one_electron_hrr",
              "pcg_one_electron_kinetic", "pcg_one_electron_contract"}
 launch_count = 0
-_RESTYPES = {"pcg_last_error": ctypes.c_char_p, "pcg_ozaki_workspace": ctypes.c_size_t}
+_RESTYPES = {"pcg_last_error": ctypes.c_char_p, "pcg_ozaki_workspace": ctypes.c_size_t,
+             "pcg_ozaki_tc_workspace": ctypes.c_size_t}
+# entry points that launch more than one kernel of this library per call
+MULTI_LAUNCH = {"pcg_ozaki_gemm_tc": 2}
 
 _lib = None
 
@@ -140,6 +147,7 @@ def call(name, *args):
     global launch_count
     if name in LAUNCHERS:
         launch_count += 1
+    launch_count += MULTI_LAUNCH.get(name, 0)
     rc = getattr(load(), name)(*args)
     check(rc, name)
     return rc

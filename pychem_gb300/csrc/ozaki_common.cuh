@@ -1,0 +1,68 @@
+// Device helpers of the Ozaki-scheme GEMMs (ozaki.cu, oz_tc.cu): the signed 7-bit
+// digit split of an FP64 value against its vector's exponent, and the exact rounding
+// of an int64 level sum times a power of two to FP64.  Integer operations only.
+#pragma once
+#include <stdint.h>
+
+#ifndef OZ_BETA
+#define OZ_BETA 7
+#endif
+
+__device__ __forceinline__ unsigned long long oz_absbits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// The NS signed digits of x for the exponent field emax of its vector's max.
+template <int NS>
+__device__ __forceinline__ void oz_digits(double x, int emax, int* d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int e = emax ? emax - 1022 : 0;  // max < 2^e
+  const int ex = (int)((u >> 52) & 0x7FF);
+  unsigned long long F = 0;
+  if (ex != 0 && emax != 0) {
+    const unsigned long long mant = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = ex - 1012 - e;  // F = mant 2^sh < 2^63
+    if (sh >= 0) F = mant << sh;
+    else if (sh > -64) F = mant >> (-sh);
+  }
+  const int lowbit = 63 - OZ_BETA * NS;  // first bit below the last digit
+#pragma unroll
+  for (int p = 1; p <= NS; ++p) d[p - 1] = (int)((F >> (63 - OZ_BETA * p)) & 127ull);
+  if (lowbit >= 1) d[NS - 1] += (int)((F >> (lowbit - 1)) & 1ull);  // round the last digit
+  int carry = 0;
+#pragma unroll
+  for (int p = NS - 1; p >= 1; --p) {
+    const int t = d[p] + carry;
+    carry = t >= 64 ? 1 : 0;
+    d[p] = t - 128 * carry;
+  }
+  d[0] += carry;
+  if ((u >> 63) != 0) {
+#pragma unroll
+    for (int p = 0; p < NS; ++p) d[p] = -d[p];
+  }
+}
+
+// acc 2^e as a double, rounded to nearest even like an int64 -> FP64 conversion, built
+// with integer operations only (64-bit conversions run on the FP64 pipe); results
+// below the normal range are flushed to 0 (far under any tolerance here).
+__device__ __forceinline__ double oz_ll_scaled(long long acc, int e) {
+  if (acc == 0) return 0.0;
+  const unsigned long long sign = acc < 0 ? 1ull : 0ull;
+  unsigned long long mag = sign ? (unsigned long long)(-acc) : (unsigned long long)acc;
+  int msb = 63 - __clzll((long long)mag);
+  unsigned long long mant;
+  if (msb <= 52) {
+    mant = mag << (52 - msb);
+  } else {
+    const int sh = msb - 52;
+    mant = mag >> sh;
+    const unsigned long long rem = mag & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+    if (mant >> 53) { mant >>= 1; ++msb; }
+  }
+  const int ef = msb + 1023 + e;
+  if (ef <= 0) return 0.0;
+  return __longlong_as_double((long long)((sign << 63) | ((unsigned long long)ef << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+

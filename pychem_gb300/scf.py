@@ -209,6 +209,45 @@ def ozaki_gemm(A, B, C, batch, M, N, K, sA, sB, sCb, nslice=6, accumulate=False)
     return C
 
 
+_TC_WS = {}
+
+
+def _tc_workspace(dev, nbytes):
+    """A cached device workspace for pcg_ozaki_gemm_tc (grown on demand)."""
+    ws = _TC_WS.get(dev)
+    if ws is None or ws.numel() < nbytes:
+        ws = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8, device=dev)
+        _TC_WS[dev] = ws
+    return ws
+
+
+def ozaki_gemm_tc(X, Y, C, M, N, K, ldx, sY, sC, nslice=6, accumulate=False):
+    """C[m*sC[0] + n*sC[1]] (+)= sum_k X[m*ldx + k] Y[k*sY[0] + n*sY[1]] in FP64 accuracy
+    with every Ozaki level in one tcgen05 tensor-core kernel (pcg_ozaki_gemm_tc); X is
+    split into BF16 digit slices on the fly.  Element offsets are relative to the
+    tensors' data pointers."""
+    import ctypes
+    from . import _lib
+    lib = _lib.load()
+    nbytes = lib.pcg_ozaki_tc_workspace(N, K, nslice)
+    ws = _tc_workspace(C.device, nbytes)
+    _lib.call("pcg_ozaki_gemm_tc", M, N, K, ctypes.c_void_p(X.data_ptr()), ldx, ctypes.c_void_p(Y.data_ptr()),
+              sY[0], sY[1], ctypes.c_void_p(C.data_ptr()), sC[0], sC[1], nslice, 1 if accumulate else 0,
+              ctypes.c_void_p(ws.data_ptr()), ws.numel(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return C
+
+
+def ozaki_tc_status(dev):
+    """Error flag of the last pcg_ozaki_gemm_tc on this device (0 = every wait ended)."""
+    import ctypes
+    from . import _lib
+    ws = _TC_WS.get(torch.device(dev) if not isinstance(dev, torch.device) else dev)
+    if ws is None:
+        return 0
+    return _lib.load().pcg_ozaki_tc_status(ctypes.c_void_p(ws.data_ptr()),
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
 def mp2_transform(eri, Co, Cv, gemm="ozaki", nslice=6, Co2=None, Cv2=None):
     """(ia|jb) from the dense AO tensor by four quarter transforms, i, a with Co, Cv
     and j, b with Co2, Cv2 (default: the same; different for the opposite-spin block
