@@ -250,23 +250,14 @@ int pcg_fock_build_noalloc(const pcg_basis_t *basis, const pcg_pairs_t *pairs, i
 int pcg_dense_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                     int ntask, const double *store, double *eri, void *stream);
 
-/* FP64-accurate batched GEMM on BF16 tensor cores by error-free operand splitting
- * (Ozaki scheme; no upstream counterpart -- it carries the AO->MO transform of
- * Methods/mp2.py:43-69).  Row-major semantics with element strides:
- *   C[b][m][n] (+)= sum_k A[b*sAb + m*sAm + k*sAk] * B[b*sBb + k*sBk + n*sBn],
- * C rows contiguous (ldc = N), batch stride sCb; a batch stride of 0 broadcasts.
- * Each operand needs a unit stride along m or k (A) and n or k (B).  nslice (1..7)
- * 7-bit slices per operand; exact FP32 level sums need K * (nslice + 2) < 4096.
- * workspace: pcg_ozaki_workspace() bytes, caller-owned device memory. */
-typedef struct {
-  int batch, M, N, K;
-  long long sAb, sAm, sAk;
-  long long sBb, sBn, sBk;
-  long long sCb;
-} pcg_gemm_desc_t;
-size_t pcg_ozaki_workspace(const pcg_gemm_desc_t *desc, int nslice);
-int pcg_ozaki_gemm(const pcg_gemm_desc_t *desc, const double *A, const double *B, double *C, int nslice,
-                   int accumulate, void *workspace, size_t ws_bytes, void *stream);
+/* The same with the bra pair packed, E[pair(a, b)][c][d] with a >= b and pair(a, b) =
+ * a(a+1)/2 + b (nbf(nbf+1)/2 x nbf x nbf doubles): the input of the first MP2
+ * quarter transform, which keeps the bra symmetry (Methods/mp2.py:43-69 transforms
+ * the full tensor). */
+int pcg_dense_pairs_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
+                          int ntask, const double *store, double *E, void *stream);
+/* out[r][a][b] = in[r][pair(a, b)] for r < R, a, b < n (pair-packed rows unpacked). */
+int pcg_unpack_pairs(long long R, int n, const double *in, double *out, void *stream);
 
 /* FP64-accurate GEMM with every Ozaki level in one tcgen05 tensor-core kernel (no
  * upstream counterpart; it carries the AO->MO transform of Methods/mp2.py:43-69 and
@@ -278,7 +269,7 @@ int pcg_ozaki_gemm(const pcg_gemm_desc_t *desc, const double *A, const double *B
  * 256-byte aligned, caller-owned device memory.  pcg_ozaki_tc_status: the error flag
  * a kernel sets when it gives up on a bounded wait (0 = none), read synchronously. */
 size_t pcg_ozaki_tc_workspace(int N, int K, int nslice);
-int pcg_ozaki_gemm_tc(int M, int N, int K, const double *X, long long ldx, const double *Y, long long sYk,
+int pcg_ozaki_gemm_tc(long long M, int N, int K, const double *X, long long ldx, const double *Y, long long sYk,
                       long long sYn, double *C, long long sCm, long long sCn, int nslice, int accumulate,
                       void *workspace, size_t ws_bytes, void *stream);
 int pcg_ozaki_tc_status(const void *workspace, void *stream);

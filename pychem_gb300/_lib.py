@@ -29,12 +29,6 @@ class BasisT(ctypes.Structure):
                 ("sh_nat", c_void_p)]
 
 
-class GemmDescT(ctypes.Structure):
-    _fields_ = [("batch", c_int), ("M", c_int), ("N", c_int), ("K", c_int),
-                ("sAb", c_longlong), ("sAm", c_longlong), ("sAk", c_longlong),
-                ("sBb", c_longlong), ("sBn", c_longlong), ("sBk", c_longlong), ("sCb", c_longlong)]
-
-
 class PairsT(ctypes.Structure):
     _fields_ = [("npair", c_int), ("npp", c_int), ("A", c_void_p), ("B", c_void_p), ("ppoff", c_void_p),
                 ("npp_of", c_void_p), ("AB", c_void_p), ("zeta", c_void_p), ("P", c_void_p), ("PA", c_void_p),
@@ -81,7 +75,6 @@ _SIGS = {
     "pcg_dense_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p,
                         c_void_p, c_void_p],
     "pcg_fma_probe": [c_int, c_int, c_int, c_int, c_void_p, c_void_p],
-    "pcg_ozaki_workspace": [ctypes.c_void_p, c_int],
     "pcg_mlp_gemm": [c_int, c_int, c_int, c_void_p, c_longlong, c_longlong, c_void_p, c_int, c_longlong, c_longlong,
                      c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p],
     "pcg_mlp_dsilu": [c_longlong, c_void_p, c_void_p, c_void_p],
@@ -91,10 +84,11 @@ _SIGS = {
                      ctypes.c_float, ctypes.c_float, c_int, c_void_p],
     "pcg_jacobi_eigh": [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_double, c_void_p,
                         c_void_p],
-    "pcg_ozaki_gemm": [ctypes.c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, ctypes.c_size_t,
-                       c_void_p],
+    "pcg_dense_pairs_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p,
+                              c_void_p, c_void_p],
+    "pcg_unpack_pairs": [c_longlong, c_int, c_void_p, c_void_p, c_void_p],
     "pcg_ozaki_tc_workspace": [c_int, c_int, c_int],
-    "pcg_ozaki_gemm_tc": [c_int, c_int, c_int, c_void_p, c_longlong, c_void_p, c_longlong, c_longlong, c_void_p,
+    "pcg_ozaki_gemm_tc": [c_longlong, c_int, c_int, c_void_p, c_longlong, c_void_p, c_longlong, c_longlong, c_void_p,
                           c_longlong, c_longlong, c_int, c_int, c_void_p, ctypes.c_size_t, c_void_p],
     "pcg_ozaki_tc_status": [c_void_p, c_void_p],
     "pcg_fock_build_noalloc": [ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_int, c_void_p, c_void_p, c_void_p,
@@ -102,15 +96,14 @@ _SIGS = {
 }
 # entry points that launch exactly one kernel of this library per call
 LAUNCHERS = {"pcg_pair_data", "pcg_pair_data_f32", "pcg_pair_ao", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
-             "pcg_digest_class", "pcg_digest_class_u", "pcg_digest_class_co", "pcg_scattering_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_ozaki_gemm", "pcg_jacobi_eigh", "pcg_mlp_gemm", "pcg_mlp_dsilu",
+             "pcg_digest_class", "pcg_digest_class_u", "pcg_digest_class_co", "pcg_scattering_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_jacobi_eigh", "pcg_dense_pairs_class", "pcg_unpack_pairs", "pcg_mlp_gemm", "pcg_mlp_dsilu",
              "pcg_mlp_colsum", "pcg_mlp_mse", "pcg_mlp_adam",
              "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",
              "pcg_two_electron_vrr", "pcg_two_electron_contract", "pcg_two_electron_hrr",
              "pcg_one_electron_fundamentals", "pcg_one_electron_vrr", "pcg_one_electron_hrr",
              "pcg_one_electron_kinetic", "pcg_one_electron_contract"}
 launch_count = 0
-_RESTYPES = {"pcg_last_error": ctypes.c_char_p, "pcg_ozaki_workspace": ctypes.c_size_t,
-             "pcg_ozaki_tc_workspace": ctypes.c_size_t}
+_RESTYPES = {"pcg_last_error": ctypes.c_char_p, "pcg_ozaki_tc_workspace": ctypes.c_size_t}
 # entry points that launch more than one kernel of this library per call
 MULTI_LAUNCH = {"pcg_ozaki_gemm_tc": 2}
 

@@ -170,6 +170,22 @@ int pcg_dense_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs,
                           (cudaStream_t)stream);
 }
 
+int pcg_dense_pairs_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                          const double* store, double* E, void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs || !E) {
+    pcg_set_error("pcg_dense_pairs_class: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  if (basis->sh_blk) { pcg_set_error("pcg_dense_pairs_class: one molecule only"); return PCG_ERR_UNSUPPORTED; }
+  return pcg_launch_dense_pairs(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, E,
+                                (cudaStream_t)stream);
+}
+
+int pcg_unpack_pairs(long long R, int n, const double* in, double* out, void* stream) {
+  if (R < 0 || n < 1 || !in || !out) { pcg_set_error("pcg_unpack_pairs: bad arguments"); return PCG_ERR_ARG; }
+  return pcg_launch_unpack_pairs(R, n, in, out, (cudaStream_t)stream);
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------------

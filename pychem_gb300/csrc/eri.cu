@@ -145,6 +145,69 @@ __global__ void k_dense(DevBasis b, DevPairsExt pr, const int2* __restrict__ tas
         }
 }
 
+// The dense tensor with the bra pair packed, E[pair(a, b)][c][d] for a >= b (pair(a, b)
+// = a(a+1)/2 + b): half of the N^4 tensor, the input of the first MP2 transform, which
+// keeps the bra symmetry; each stored element goes to its four images with a >= b.
+__device__ __forceinline__ size_t ao_pair(size_t a, size_t b) { return a >= b ? a * (a + 1) / 2 + b : b * (b + 1) / 2 + a; }
+
+template <int NA, int NB, int NC, int ND>
+__global__ void k_dense_pairs(DevBasis b, DevPairsExt pr, const int2* __restrict__ tasks, int ntask,
+                              const double* __restrict__ store, double* __restrict__ E) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  const int2 tk = tasks[t];
+  const int oa = b.sh_ao[pr.p.A[tk.x]], ob = b.sh_ao[pr.p.B[tk.x]];
+  const int oc = b.sh_ao[pr.p.A[tk.y]], od = b.sh_ao[pr.p.B[tk.y]];
+  const size_t n = b.nbf;
+  for (int i = 0; i < NA; ++i)
+    for (int j = 0; j < NB; ++j) {
+      const size_t pab = ao_pair(oa + i, ob + j);
+      for (int k = 0; k < NC; ++k)
+        for (int l = 0; l < ND; ++l) {
+          const double v = store[(size_t)(((i * NB + j) * NC + k) * ND + l) * ntask + t];
+          const size_t a = oa + i, bb = ob + j, c = oc + k, d = od + l;
+          const size_t pcd = ao_pair(c, d);
+          E[(pab * n + c) * n + d] = v;
+          E[(pab * n + d) * n + c] = v;
+          E[(pcd * n + a) * n + bb] = v;
+          E[(pcd * n + bb) * n + a] = v;
+        }
+    }
+}
+
+// out[r][a][b] = in[r][pair(a, b)] for r < R, a, b < n
+__global__ void k_unpack_pairs(long long R, int n, const double* __restrict__ in, double* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nn = (long long)n * n;
+  if (idx >= R * nn) return;
+  const long long r = idx / nn;
+  const int ab = (int)(idx - r * nn), a = ab / n, bb = ab - a * n;
+  out[idx] = __ldg(in + r * (nn + n) / 2 + ao_pair(a, bb));
+}
+
+int pcg_launch_dense_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
+                           const double* store, double* E, cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  const int threads = 128, blocks = (ntask + threads - 1) / threads;
+  switch (cls) {
+#define X(id, a, bb, c, d) \
+  case id: k_dense_pairs<a, bb, c, d><<<blocks, threads, 0, s>>>(b, pr, tasks, ntask, store, E); break;
+    PCG_SHAPE_CASES(X)
+#undef X
+    default: pcg_set_error("pcg_dense_pairs_class: class id out of range"); return PCG_ERR_ARG;
+  }
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+int pcg_launch_unpack_pairs(long long R, int n, const double* in, double* out, cudaStream_t s) {
+  const long long total = R * n * n;
+  if (total <= 0) return PCG_OK;
+  k_unpack_pairs<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(R, n, in, out);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
 // Schwarz factor per shell pair from its diagonal block (ab|ab): sqrt(max (mn|mn)),
 // the upstream bound of hartree_fock.py:244-254 reduced to the pair level.
 template <int NA, int NB>

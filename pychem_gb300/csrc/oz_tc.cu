@@ -15,8 +15,10 @@
 //    X in global memory).  The exponent of each row comes from a first pass over the
 //    CTA's rows (the re-read is served by L2).
 //  * Y, the small operand (C_occ or C_vir: a few hundred columns), is split once by
-//    k_ozt_split_y into K-major BF16 slices in the caller's workspace and copied tile by
-//    tile into shared memory by the same producer warps.
+//    k_ozt_split_y into K-major BF16 slices in the caller's workspace (slice-major,
+//    [p][n][k]) and brought into shared memory tile by tile by the tensor memory
+//    accelerator (cp.async.bulk.tensor, 64-byte swizzle, completion counted on the
+//    stage's mbarrier).
 //  * One thread issues tcgen05.mma (M = 128, N = BN, K = 16, BF16 in, FP32 out) for
 //    every slice pair with p + q <= NS + 1 into NS accumulators in tensor memory, one
 //    per level (NS * BN <= 512 columns), over a two-stage mbarrier pipeline.
@@ -27,6 +29,8 @@
 // Level sums are exact while K (NS + 2) < 4096.  Every mbarrier wait is bounded; a CTA
 // that gives up sets the error flag in the workspace, drains its MMAs, frees its
 // tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <stdio.h>
 
@@ -58,7 +62,7 @@ struct OztWs {  // workspace header (device): error flag, then exponents of Y an
   int err;
 };
 
-// Y slices: ys[(n * NS + p) * Kp + k] (BF16, zero for k >= K and n >= N), ey[n]: one
+// Y slices: ys[(p * Npad + n) * Kp + k] (BF16, zero for k >= K and n >= N), ey[n]: one
 // warp per column n, lanes over k.
 template <int NS>
 __global__ void k_ozt_split_y(const double* __restrict__ Y, long long sYk, long long sYn, int K, int N, int Npad,
@@ -66,9 +70,10 @@ __global__ void k_ozt_split_y(const double* __restrict__ Y, long long sYk, long 
   const int n = blockIdx.x * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (n >= Npad) return;
-  __nv_bfloat16* out = ys + (size_t)n * NS * Kp;
+  __nv_bfloat16* out = ys + (size_t)n * Kp;
+  const size_t pstride = (size_t)Npad * Kp;
   if (n >= N) {
-    for (int i = lane; i < NS * Kp; i += 32) out[i] = __float2bfloat16(0.0f);
+    for (int i = lane; i < NS * Kp; i += 32) out[(i / Kp) * pstride + i % Kp] = __float2bfloat16(0.0f);
     if (lane == 0) ey[n] = 0;
     return;
   }
@@ -87,31 +92,71 @@ __global__ void k_ozt_split_y(const double* __restrict__ Y, long long sYk, long 
       for (int p = 0; p < NS; ++p) d[p] = 0;
     }
 #pragma unroll
-    for (int p = 0; p < NS; ++p) out[(size_t)p * Kp + k] = __int2bfloat16_rn(d[p]);
+    for (int p = 0; p < NS; ++p) out[p * pstride + k] = __int2bfloat16_rn(d[p]);
   }
+}
+
+// the 8 consecutive FP64 values of row m from column kb (zero outside [0, K) or m >= M)
+__device__ __forceinline__ void ozt_load8(const double* __restrict__ X, long long ldx, long long m, long long M, int kb,
+                                          int K, bool vec, double (&v)[8]) {
+  if (m < M && vec && kb + 8 <= K) {
+    const double2* src = (const double2*)(X + m * ldx + kb);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const double2 q = __ldg(src + h);
+      v[2 * h] = q.x;
+      v[2 * h + 1] = q.y;
+    }
+  } else if (m < M) {
+    const double* src = X + m * ldx + kb;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = (kb + j < K) ? __ldg(src + j) : 0.0;
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = 0.0;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
 template <int NS, int BN>
 __global__ void __launch_bounds__(OZT_THREADS, 1)
-    k_ozt_gemm(int M, int N, int K, int Kp, const double* __restrict__ X, long long ldx,
-               const __nv_bfloat16* __restrict__ ys, const int* __restrict__ ey, double* __restrict__ C, long long sCm,
-               long long sCn, int accumulate, int* __restrict__ err) {
+    k_ozt_gemm(long long M, int N, int K, int Kp, int Npad, const double* __restrict__ X, long long ldx,
+               const __grid_constant__ CUtensorMap ymap, const int* __restrict__ ey, double* __restrict__ C,
+               long long sCm, long long sCn, int accumulate, int* __restrict__ err) {
   using Cfg = OztCfg<NS, BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* tiles = sm;                                        // [stage][X slices | Y slices]
-  uint64_t* bars = (uint64_t*)(sm + 2 * Cfg::STAGE);          // full[2], empty[2], done, drain
-  uint32_t* tmem_slot = (uint32_t*)(bars + 6);
+  uint64_t* bars = (uint64_t*)(sm + 2 * Cfg::STAGE);  // full[2], empty[2], done, drain, ycopy[2]
+  uint32_t* tmem_slot = (uint32_t*)(bars + 8);
   volatile int* abort_s = (volatile int*)(tmem_slot + 1);
   int* ex_s = (int*)(tmem_slot + 4);                           // 128 row exponent fields
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * OZT_BM;
-  const int n0 = blockIdx.x * BN;
+  // linear grid, the N tiles of one row tile adjacent (they share its X rows in L2)
+  const int ntn = (N + BN - 1) / BN;
+  const long long m0 = (long long)(blockIdx.x / ntn) * OZT_BM;
+  const int n0 = (int)(blockIdx.x % ntn) * BN;
   const int nchunk = Kp / OZT_BK;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 2; ++i) { mbar_init(&bars[i], OZT_PROD); mbar_init(&bars[2 + i], 1); }
+    // full: every producer thread; ycopy: the expect_tx arrival of the thread that issues
+    // the Y copies, completed by their bytes
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&bars[i], OZT_PROD);
+      mbar_init(&bars[2 + i], 1);
+      mbar_init(&bars[6 + i], 1);
+    }
     mbar_init(&bars[4], 1);
     mbar_init(&bars[5], 1);
     *abort_s = 0;
@@ -124,71 +169,96 @@ __global__ void __launch_bounds__(OZT_THREADS, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp < OZT_PROD_WARPS) {
-    // ---- exponents of the CTA's 128 rows of X
-    for (int r = warp; r < OZT_BM; r += OZT_PROD_WARPS) {
-      const int m = m0 + r;
+    const int t = threadIdx.x;
+    const bool vec = (ldx % 2 == 0) && (((uintptr_t)X & 15) == 0);
+    // ---- exponents of the CTA's 128 rows of X: two threads per row, each over half
+    // of the row (an even split, so 16-byte loads stay aligned), many loads in flight
+    {
+      const int r = t >> 1, h = t & 1;
+      const long long m = m0 + r;
+      const int kh = ((K + 1) / 2 + 1) & ~1;
+      const int klo = h ? kh : 0, khi = h ? K : (kh < K ? kh : K);
       unsigned long long mx = 0;
-      if (m < M)
-        for (int k = lane; k < K; k += 32) mx = max(mx, oz_absbits(__ldg(X + (long long)m * ldx + k)));
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      if (lane == 0) ex_s[r] = (int)(mx >> 52);
+      if (m < M && klo < khi) {
+        const double* row = X + m * ldx;
+        int k = klo;
+        if (vec) {
+#pragma unroll 8
+          for (; k + 2 <= khi; k += 2) {
+            const double2 q = __ldg((const double2*)(row + k));
+            mx = max(mx, max(oz_absbits(q.x), oz_absbits(q.y)));
+          }
+        }
+        for (; k < khi; ++k) mx = max(mx, oz_absbits(__ldg(row + k)));
+      }
+      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+      if (h == 0) ex_s[r] = (int)(mx >> 52);
     }
     asm volatile("bar.sync 1, %0;" ::"r"(OZT_PROD));
-    const int t = threadIdx.x;
+    // this thread's two 8-column items of every chunk: rows r0, r0 + 64, group g
+    const int g = t & 3, r0 = t >> 2;
+    const int e0 = ex_s[r0], e1 = ex_s[r0 + 64];
+    double va[8], vb[8];
+    ozt_load8(X, ldx, m0 + r0, M, 8 * g, K, vec, va);
+    ozt_load8(X, ldx, m0 + r0 + 64, M, 8 * g, K, vec, vb);
     bool ok = true;
-    for (int c = 0; c < nchunk && ok; ++c) {
+    int ycopies[2] = {0, 0};  // Y copies issued per stage (thread 0)
+    for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
       if (c >= 2 && !mbar_wait(&bars[2 + st], ((c >> 1) + 1) & 1, OZT_WAIT, abort_s)) { ok = false; break; }
       uint8_t* xt = tiles + st * Cfg::STAGE;
       uint8_t* yt = xt + NS * Cfg::XT;
       const int k0 = c * OZT_BK;
-      // X: 128 rows x 4 groups of 8 columns; item i -> row i / 4, group i % 4
+      if (t == 0) {  // Y slices of this chunk by TMA
+        ++ycopies[st];
+        mbar_arrive_expect_tx(&bars[6 + st], NS * Cfg::YT);
 #pragma unroll 1
-      for (int i = t; i < OZT_BM * 4; i += OZT_PROD) {
-        const int r = i >> 2, g = i & 3, m = m0 + r;
-        const int kb = k0 + 8 * g;
-        double v[8];
-        if (m < M) {
-          const double* src = X + (long long)m * ldx + kb;
+        for (int p = 0; p < NS; ++p) tma_load_2d(smem_u32(yt + p * Cfg::YT), &ymap, k0, p * Npad + n0, &bars[6 + st]);
+      }
+      // prefetch the next chunk's values while this one is split
+      double na[8], nb[8];
+      if (c + 1 < nchunk) {
+        ozt_load8(X, ldx, m0 + r0, M, k0 + OZT_BK + 8 * g, K, vec, na);
+        ozt_load8(X, ldx, m0 + r0 + 64, M, k0 + OZT_BK + 8 * g, K, vec, nb);
+      }
 #pragma unroll
-          for (int j = 0; j < 8; ++j) v[j] = (kb + j < K) ? __ldg(src + j) : 0.0;
-        } else {
-#pragma unroll
-          for (int j = 0; j < 8; ++j) v[j] = 0.0;
-        }
-        const int emax = ex_s[r];
+      for (int it = 0; it < 2; ++it) {
+        const int r = it ? r0 + 64 : r0;
+        const int emax = it ? e1 : e0;
         int d[8][NS];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) oz_digits<NS>(v[j], emax, d[j]);
+        for (int j = 0; j < 8; ++j) oz_digits<NS>(it ? vb[j] : va[j], emax, d[j]);
         const uint32_t off = sw64_offset(r, g);
 #pragma unroll
         for (int p = 0; p < NS; ++p) {
           uint32_t w[4];
 #pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            __nv_bfloat162 b2 = __halves2bfloat162(__int2bfloat16_rn(d[2 * h][p]), __int2bfloat16_rn(d[2 * h + 1][p]));
-            w[h] = *(uint32_t*)&b2;
+          for (int hh = 0; hh < 4; ++hh) {
+            __nv_bfloat162 b2 = __halves2bfloat162(__int2bfloat16_rn(d[2 * hh][p]), __int2bfloat16_rn(d[2 * hh + 1][p]));
+            w[hh] = *(uint32_t*)&b2;
           }
           *(uint4*)(xt + p * Cfg::XT + off) = make_uint4(w[0], w[1], w[2], w[3]);
         }
       }
-      // Y: NS slices x BN rows x 4 chunks of 16 bytes
-#pragma unroll 1
-      for (int i = t; i < NS * BN * 4; i += OZT_PROD) {
-        const int ch = i & 3, n = (i >> 2) % BN, p = (i >> 2) / BN;
-        const uint4 q = __ldg((const uint4*)(ys + ((size_t)(n0 + n) * NS + p) * Kp + k0) + ch);
-        *(uint4*)(yt + p * Cfg::YT + sw64_offset(n, ch)) = q;
-      }
       fence_proxy_async_smem();
       mbar_arrive(&bars[st]);
+      if (c + 1 < nchunk) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { va[j] = na[j]; vb[j] = nb[j]; }
+      }
     }
     if (!ok) { *abort_s = 1; atomicExch(err, 1); }
+    if (t == 0 && *abort_s) {  // let this thread's Y copies land before the CTA exits
+      volatile int keep_waiting = 0;
+      for (int i = 0; i < 2; ++i)
+        if (ycopies[i]) mbar_wait(&bars[6 + i], (ycopies[i] - 1) & 1, OZT_WAIT, &keep_waiting);
+    }
     // ---- epilogue: wait for the last MMAs, combine the levels, write C
     if (ok && mbar_wait(&bars[4], 0, OZT_WAIT, abort_s)) {
       tc_fence_after();
       const int lg = warp & 3, half = warp >> 2;
-      const int r = 32 * lg + lane, m = m0 + r;
+      const int r = 32 * lg + lane;
+      const long long m = m0 + r;
       const int emax = ex_s[r];
       const int ex = (emax ? emax - 1022 : 0) - OZ_BETA * (NS + 1);
       const uint32_t trow = tmem + ((uint32_t)(32 * lg) << 16);
@@ -207,7 +277,7 @@ __global__ void __launch_bounds__(OZT_THREADS, 1)
 #pragma unroll
             for (int L = 0; L < NS; ++L) acc += (long long)__float2int_rn(P[L][j]) << (OZ_BETA * (NS - 1 - L));
             const double val = oz_ll_scaled(acc, ex + __ldg(ey + n));
-            double* cp = C + (long long)m * sCm + (long long)n * sCn;
+            double* cp = C + m * sCm + (long long)n * sCn;
             *cp = accumulate ? *cp + val : val;
           }
         }
@@ -223,7 +293,11 @@ __global__ void __launch_bounds__(OZT_THREADS, 1)
     bool ok = true;
     for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
-      if (!mbar_wait(&bars[st], (c >> 1) & 1, OZT_WAIT, abort_s)) { ok = false; break; }
+      if (!mbar_wait(&bars[st], (c >> 1) & 1, OZT_WAIT, abort_s) ||
+          !mbar_wait(&bars[6 + st], (c >> 1) & 1, OZT_WAIT, abort_s)) {
+        ok = false;
+        break;
+      }
       tc_fence_after();
       const uint32_t xa = smem_u32(tiles + st * Cfg::STAGE);
       const uint32_t ya = xa + NS * Cfg::XT;
@@ -285,8 +359,28 @@ static OztLayout ozt_layout(int N, int K, int nslice) {
   return L;
 }
 
+typedef CUresult (*PcgEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int get_encode_tiled(PcgEncodeTiled* fn) {
+  static PcgEncodeTiled cached = nullptr;
+  if (!cached) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p) {
+      pcg_set_error("cuTensorMapEncodeTiled not available from the driver");
+      return PCG_ERR_CUDA;
+    }
+    cached = (PcgEncodeTiled)p;
+  }
+  *fn = cached;
+  return PCG_OK;
+}
+
 template <int NS, int BN>
-static int ozt_run(int M, int N, int K, const double* X, long long ldx, const double* Y, long long sYk, long long sYn,
+static int ozt_run(long long M, int N, int K, const double* X, long long ldx, const double* Y, long long sYk, long long sYn,
                    double* C, long long sCm, long long sCn, int accumulate, char* ws, const OztLayout& L,
                    cudaStream_t s) {
   using Cfg = OztCfg<NS, BN>;
@@ -295,6 +389,22 @@ static int ozt_run(int M, int N, int K, const double* X, long long ldx, const do
   __nv_bfloat16* ys = (__nv_bfloat16*)(ws + L.off_ys);
   k_ozt_split_y<NS><<<(L.Npad + 7) / 8, 256, 0, s>>>(Y, sYk, sYn, K, N, L.Npad, L.Kp, ys, ey);
   PCG_CUDA(cudaGetLastError());
+  // Y slices as a 2-D tensor [NS * Npad rows][Kp columns] of BF16; boxes of 32 columns
+  // (64 bytes, the swizzle span) by BN rows; k0 is a multiple of 32, so every copy
+  // starts on a 64-byte boundary
+  PcgEncodeTiled encode;
+  if (int rc = get_encode_tiled(&encode)) return rc;
+  CUtensorMap ymap;
+  const cuuint64_t gdim[2] = {(cuuint64_t)L.Kp, (cuuint64_t)NS * L.Npad};
+  const cuuint64_t gstride[1] = {(cuuint64_t)L.Kp * 2};
+  const cuuint32_t box[2] = {OZT_BK, BN};
+  const cuuint32_t estr[2] = {1, 1};
+  if (encode(&ymap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)ys, gdim, gstride, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+    pcg_set_error("pcg_ozaki_gemm_tc: cuTensorMapEncodeTiled rejected the Y slice layout");
+    return PCG_ERR_CUDA;
+  }
   static bool attr_set[64];
   int dev = 0;
   PCG_CUDA(cudaGetDevice(&dev));
@@ -302,9 +412,9 @@ static int ozt_run(int M, int N, int K, const double* X, long long ldx, const do
     PCG_CUDA(cudaFuncSetAttribute(k_ozt_gemm<NS, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM));
     attr_set[dev] = true;
   }
-  dim3 grid(L.Npad / BN, (M + OZT_BM - 1) / OZT_BM);
-  k_ozt_gemm<NS, BN><<<grid, OZT_THREADS, Cfg::SMEM, s>>>(M, N, K, L.Kp, X, ldx, ys, ey, C, sCm, sCn, accumulate,
-                                                         err);
+  const long long blocks = (long long)(L.Npad / BN) * ((M + OZT_BM - 1) / OZT_BM);
+  k_ozt_gemm<NS, BN><<<(unsigned)blocks, OZT_THREADS, Cfg::SMEM, s>>>(M, N, K, L.Kp, L.Npad, X, ldx, ymap, ey, C, sCm,
+                                                                    sCn, accumulate, err);
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;
 }
@@ -314,7 +424,7 @@ extern "C" size_t pcg_ozaki_tc_workspace(int N, int K, int nslice) {
   return ozt_layout(N, K, nslice).total;
 }
 
-extern "C" int pcg_ozaki_gemm_tc(int M, int N, int K, const double* X, long long ldx, const double* Y, long long sYk,
+extern "C" int pcg_ozaki_gemm_tc(long long M, int N, int K, const double* X, long long ldx, const double* Y, long long sYk,
                                  long long sYn, double* C, long long sCm, long long sCn, int nslice, int accumulate,
                                  void* workspace, size_t ws_bytes, void* stream) {
   if (M < 1 || N < 1 || K < 1 || !X || !Y || !C || ldx < K) {
@@ -329,11 +439,11 @@ extern "C" int pcg_ozaki_gemm_tc(int M, int N, int K, const double* X, long long
     pcg_set_error("pcg_ozaki_gemm_tc: K too large for exact FP32 level sums (need K * (nslice + 2) < 4096)");
     return PCG_ERR_UNSUPPORTED;
   }
-  if ((long long)(M + OZT_BM - 1) / OZT_BM > 65535) {
-    pcg_set_error("pcg_ozaki_gemm_tc: M too large for one launch (at most 65535 * 128 rows)");
+  const OztLayout L = ozt_layout(N, K, nslice);
+  if ((M + OZT_BM - 1) / OZT_BM * (long long)(L.Npad / L.BN) >= (1ll << 31)) {
+    pcg_set_error("pcg_ozaki_gemm_tc: M too large for one launch");
     return PCG_ERR_UNSUPPORTED;
   }
-  const OztLayout L = ozt_layout(N, K, nslice);
   if (!workspace || ws_bytes < L.total || ((size_t)workspace & 255)) {
     pcg_set_error("pcg_ozaki_gemm_tc: workspace missing, too small or not 256-byte aligned (query pcg_ozaki_tc_workspace)");
     return PCG_ERR_CAPACITY;

@@ -403,6 +403,17 @@ class GpuEngine:
                           _stream())
         return 0.25 * (GJ + GJ.transpose(1, 2)), -0.5 * GK
 
+    def dense_eri_pairs(self):
+        """The dense tensor with the bra pair packed: E[pair(a, b)][c][d], a >= b,
+        pair(a, b) = a(a+1)/2 + b (nbf(nbf+1)/2 x nbf x nbf), zero where screened out."""
+        n = self.nbf
+        E = torch.zeros(n * (n + 1) // 2 * n * n, dtype=torch.float64, device=self.dev)
+        for cls, rec in self.classes.items():
+            for part, (tasks, ntask) in rec.items():
+                _lib.call("pcg_dense_pairs_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
+                          _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), _ptr(E), _stream())
+        return E.view(n * (n + 1) // 2, n, n)
+
     def dense_eri(self):
         """Dense nbf^4 tensor (8-fold symmetric fill), zero where screened out."""
         n = self.nbf

@@ -17,7 +17,8 @@ non-variational and lets its loop report energies of diverged runs), and converg
 needs both |dE| < ``e_tol`` and RMS(dD) < ``d_tol`` (upstream: |dE| < 1e-7 only).
 
 RMP2 is the closed-shell form of ``Methods/mp2.py:43-94`` (identical value for RHF);
-the AO->MO transforms run on BF16 tensor cores with FP64 accuracy (ozaki_gemm).
+the AO->MO transforms run on the tcgen05 tensor cores with FP64 accuracy
+(ozaki_gemm_tc: Ozaki digit slices, every level in one kernel).
 """
 import math
 import time
@@ -195,20 +196,6 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                      converged=converged, history=history, fock_builds=it)
 
 
-def ozaki_gemm(A, B, C, batch, M, N, K, sA, sB, sCb, nslice=6, accumulate=False):
-    """C[b][m][n] (+)= sum_k A[b,m,k] B[b,k,n] in FP64 accuracy on BF16 tensor cores
-    (pcg_ozaki_gemm); sA = (sAb, sAm, sAk), sB = (sBb, sBk, sBn) element strides."""
-    import ctypes
-    from . import _lib
-    d = _lib.GemmDescT(batch, M, N, K, sA[0], sA[1], sA[2], sB[0], sB[2], sB[1], sCb)
-    nbytes = _lib.load().pcg_ozaki_workspace(ctypes.byref(d), nslice)
-    ws = torch.empty(nbytes, dtype=torch.uint8, device=C.device)
-    _lib.call("pcg_ozaki_gemm", ctypes.byref(d), ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
-              ctypes.c_void_p(C.data_ptr()), nslice, 1 if accumulate else 0, ctypes.c_void_p(ws.data_ptr()), nbytes,
-              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
-    return C
-
-
 _TC_WS = {}
 
 
@@ -248,47 +235,74 @@ def ozaki_tc_status(dev):
                                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
 
 
-def mp2_transform(eri, Co, Cv, gemm="ozaki", nslice=6, Co2=None, Cv2=None):
-    """(ia|jb) from the dense AO tensor by four quarter transforms, i, a with Co, Cv
-    and j, b with Co2, Cv2 (default: the same; different for the opposite-spin block
-    of UMP2).  gemm="fp64": cuBLAS DGEMM; gemm="ozaki": BF16 tensor cores with FP64
-    accuracy."""
+def _pair_rows(n, dev):
+    """Row index a*n + b of every AO pair a >= b in pair order (pair(a, b) = a(a+1)/2 + b)."""
+    a, b = torch.tril_indices(n, n, device=dev)
+    return a * n + b
+
+
+def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None):
+    """(ia|jb) from the AO integrals by four quarter transforms, i, a with Co, Cv and
+    j, b with Co2, Cv2 (default: the same; different for the opposite-spin block of
+    UMP2).  eri: the dense tensor (n, n, n, n) or the bra-pair-packed one
+    (n(n+1)/2, n, n) of GpuEngine.dense_eri_pairs.
+
+    gemm="tc": each transform is one pcg_ozaki_gemm_tc launch (FP64-accurate on the
+    tcgen05 tensor cores) contracting the last, contiguous index of its input and
+    writing its output transposed, so that the next transform again contracts a
+    contiguous index; the first two keep the bra pair packed (ab) = (ba):
+        T1[i][ab c] = sum_d (ab|cd) Co[d][i]          T2[a'][i ab] = sum_c T1 Cv[c][a']
+        T2 unpacked to [a'][i][a][b]                   T3[j][a' i a] = sum_b T2 Co2[b][j]
+        T4[b'][j a' i] = sum_a T3 Cv2[a][b']           T4[b'][j][a'][i] = (i a'|j b').
+    gemm="fp64": the same contraction by FP64 matrix products on the dense tensor
+    (cuBLAS DGEMM through torch), the cross-check."""
     n, o = Co.shape
     v = Cv.shape[1]
     Co2 = Co if Co2 is None else Co2
     Cv2 = Cv if Cv2 is None else Cv2
     o2, v2 = Co2.shape[1], Cv2.shape[1]
+    npair = n * (n + 1) // 2
     if gemm == "fp64":
+        if eri.dim() != 4:
+            raise ValueError("gemm='fp64' needs the dense (n, n, n, n) tensor")
         t1 = (Co.T @ eri.reshape(n, n ** 3)).reshape(o, n, n * n)        # (i nu | lam sig)
         t2 = torch.matmul(Cv.T, t1)                                       # (i a | lam sig)
         del t1
         t3 = torch.matmul(Co2.T, t2.reshape(o * v, n, n))                 # (i a | j sig)
         del t2
         return torch.matmul(t3, Cv2).reshape(o, v, o2, v2)                # (i a | j b)
+    if gemm != "tc":
+        raise ValueError("gemm must be 'tc' or 'fp64'")
     dev = eri.device
+    import ctypes
+    from . import _lib
+    if eri.dim() == 4:
+        eri = eri.reshape(n * n, n * n)[_pair_rows(n, dev)]
     E = eri.reshape(-1)
     Co, Cv, Co2, Cv2 = Co.contiguous(), Cv.contiguous(), Co2.contiguous(), Cv2.contiguous()
-    # Y1[i][(b c d)] = sum_a Co[a][i] E[a][(b c d)]
-    Y1 = torch.empty(o * n ** 3, dtype=torch.float64, device=dev)
-    ozaki_gemm(Co, E, Y1, 1, o, n ** 3, n, (0, 1, o), (0, n ** 3, 1), 0, nslice)
-    # Y2[i][a'][(c d)] = sum_b Cv[b][a'] Y1[i][b][(c d)]
-    Y2 = torch.empty(o * v * n * n, dtype=torch.float64, device=dev)
-    ozaki_gemm(Cv, Y1, Y2, o, v, n * n, n, (0, 1, v), (n ** 3, n * n, 1), v * n * n, nslice)
-    del Y1
-    # Y3[(i a)][j][d] = sum_c Co2[c][j] Y2[(i a)][c][d]
-    Y3 = torch.empty(o * v * o2 * n, dtype=torch.float64, device=dev)
-    ozaki_gemm(Co2, Y2, Y3, o * v, o2, n, n, (0, 1, o2), (n * n, n, 1), o2 * n, nslice)
-    del Y2
-    # T[(i a j)][b] = sum_d Y3[(i a j)][d] Cv2[d][b]
-    T = torch.empty(o * v * o2 * v2, dtype=torch.float64, device=dev)
-    ozaki_gemm(Y3, Cv2, T, 1, o * v * o2, v2, n, (0, n, 1), (0, v2, 1), 0, nslice)
-    return T.reshape(o, v, o2, v2)
+
+    def quarter(X, rows, C, ncol):
+        out = torch.empty(ncol * rows, dtype=torch.float64, device=dev)
+        ozaki_gemm_tc(X, C, out, rows, ncol, n, n, (ncol, 1), (1, rows), nslice=nslice)
+        return out
+
+    T1 = quarter(E, npair * n, Co, o)
+    T2p = quarter(T1, o * npair, Cv, v)
+    del T1
+    T2 = torch.empty(v * o * n * n, dtype=torch.float64, device=dev)
+    _lib.call("pcg_unpack_pairs", v * o, n, ctypes.c_void_p(T2p.data_ptr()), ctypes.c_void_p(T2.data_ptr()),
+              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    del T2p
+    T3 = quarter(T2, v * o * n, Co2, o2)
+    del T2
+    T4 = quarter(T3, o2 * v * o, Cv2, v2)
+    return T4.view(v2, o2, v, o).permute(3, 2, 1, 0)
 
 
 MP2_SCALES = {"MP2": None, "MP2-SCS": (1.0 / 3.0, 6.0 / 5.0), "MP2-SOS": (0.0, 1.3)}   # Methods/mp2.py:97-107
 
 
-def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6, scale=None):
+def rmp2(engine, C, eps, eri=None, gemm="tc", nslice=6, scale=None):
     """Closed-shell MP2 correlation energy: four quarter transforms of the dense AO
     tensor to (ia|jb) and the energy denominator sum.  scale = (c_ss, c_os) weights
     the same-spin part sum (ia|jb)((ia|jb) - (ib|ja))/D and the opposite-spin part
@@ -296,7 +310,7 @@ def rmp2(engine, C, eps, eri=None, gemm="ozaki", nslice=6, scale=None):
     mol = engine.mol
     o = mol.NAlphaElectrons
     if eri is None:
-        eri = engine.dense_eri()
+        eri = engine.dense_eri() if gemm == "fp64" else engine.dense_eri_pairs()
     Co = C[:, :o].contiguous()
     Cv = C[:, o:].contiguous()
     ovov = mp2_transform(eri, Co, Cv, gemm=gemm, nslice=nslice)
@@ -475,7 +489,7 @@ def uhf(engine, cuhf=False, max_iter=300, e_tol=1e-10, d_tol=1e-8, C0=None, mom=
                      converged=converged)
 
 
-def ump2(engine, res, eri=None, gemm="ozaki", nslice=6, scale=None):
+def ump2(engine, res, eri=None, gemm="tc", nslice=6, scale=None):
     """Unrestricted MP2 correlation energy (Methods/mp2.py:43-101): same-spin
     0.25 sum ((ia|jb) - (ib|ja))^2 / D per spin and opposite-spin sum (ia|jb)^2 / D,
     with the orbital energies of the final Fock matrices; the integrals from the four
@@ -484,7 +498,7 @@ def ump2(engine, res, eri=None, gemm="ozaki", nslice=6, scale=None):
     mol = engine.mol
     na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
     if eri is None:
-        eri = engine.dense_eri()
+        eri = engine.dense_eri() if gemm == "fp64" else engine.dense_eri_pairs()
     Ca, Cb, ea, eb = res.Ca, res.Cb, res.ea, res.eb
 
     def same(C, e, o):
