@@ -9,7 +9,7 @@
 // int64.  What this kernel changes is where the work happens:
 //
 //  * X, the large operand (millions of rows in the MP2 transforms), is read once as
-//    FP64 from global memory and split on the fly: eight producer warps load a 128-row
+//    FP64 from global memory and split on the fly: sixteen producer warps load a 128-row
 //    by 32-column chunk, cut it into NS digit slices and store them BF16, K-major and
 //    64-byte swizzled, straight into the shared-memory operand tiles (no BF16 copy of
 //    X in global memory).  The exponent of each row comes from a first pass over the
@@ -42,7 +42,7 @@
 
 #define OZT_BM 128
 #define OZT_BK 32
-#define OZT_PROD_WARPS 8
+#define OZT_PROD_WARPS 16
 #define OZT_PROD (OZT_PROD_WARPS * 32)
 #define OZT_THREADS (OZT_PROD + 32)
 #define OZT_WAIT (1u << 24)
@@ -171,13 +171,13 @@ __global__ void __launch_bounds__(OZT_THREADS, 1)
   if (warp < OZT_PROD_WARPS) {
     const int t = threadIdx.x;
     const bool vec = (ldx % 2 == 0) && (((uintptr_t)X & 15) == 0);
-    // ---- exponents of the CTA's 128 rows of X: two threads per row, each over half
-    // of the row (an even split, so 16-byte loads stay aligned), many loads in flight
+    // ---- exponents of the CTA's 128 rows of X: four threads per row, each over a
+    // quarter of the row (even boundaries, so 16-byte loads stay aligned)
     {
-      const int r = t >> 1, h = t & 1;
+      const int r = t >> 2, h = t & 3;
       const long long m = m0 + r;
-      const int kh = ((K + 1) / 2 + 1) & ~1;
-      const int klo = h ? kh : 0, khi = h ? K : (kh < K ? kh : K);
+      const int kq = ((K + 3) / 4 + 1) & ~1;
+      const int klo = h * kq < K ? h * kq : K, khi = (h + 1) * kq < K ? (h + 1) * kq : K;
       unsigned long long mx = 0;
       if (m < M && klo < khi) {
         const double* row = X + m * ldx;
@@ -192,60 +192,52 @@ __global__ void __launch_bounds__(OZT_THREADS, 1)
         for (; k < khi; ++k) mx = max(mx, oz_absbits(__ldg(row + k)));
       }
       mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
       if (h == 0) ex_s[r] = (int)(mx >> 52);
     }
     asm volatile("bar.sync 1, %0;" ::"r"(OZT_PROD));
-    // this thread's two 8-column items of every chunk: rows r0, r0 + 64, group g
-    const int g = t & 3, r0 = t >> 2;
-    const int e0 = ex_s[r0], e1 = ex_s[r0 + 64];
-    double va[8], vb[8];
-    ozt_load8(X, ldx, m0 + r0, M, 8 * g, K, vec, va);
-    ozt_load8(X, ldx, m0 + r0 + 64, M, 8 * g, K, vec, vb);
+    // this thread's 8-column item of every chunk: row r, column group g
+    const int g = t & 3, r = t >> 2;
+    const int emax = ex_s[r];
+    const uint32_t off = sw64_offset(r, g);
     bool ok = true;
     int ycopies[2] = {0, 0};  // Y copies issued per stage (thread 0)
     for (int c = 0; c < nchunk; ++c) {
       const int st = c & 1;
+      const int k0 = c * OZT_BK;
+      double v[8];
+      ozt_load8(X, ldx, m0 + r, M, k0 + 8 * g, K, vec, v);   // issued before the wait
       if (c >= 2 && !mbar_wait(&bars[2 + st], ((c >> 1) + 1) & 1, OZT_WAIT, abort_s)) { ok = false; break; }
       uint8_t* xt = tiles + st * Cfg::STAGE;
       uint8_t* yt = xt + NS * Cfg::XT;
-      const int k0 = c * OZT_BK;
       if (t == 0) {  // Y slices of this chunk by TMA
         ++ycopies[st];
         mbar_arrive_expect_tx(&bars[6 + st], NS * Cfg::YT);
 #pragma unroll 1
         for (int p = 0; p < NS; ++p) tma_load_2d(smem_u32(yt + p * Cfg::YT), &ymap, k0, p * Npad + n0, &bars[6 + st]);
       }
-      // prefetch the next chunk's values while this one is split
-      double na[8], nb[8];
-      if (c + 1 < nchunk) {
-        ozt_load8(X, ldx, m0 + r0, M, k0 + OZT_BK + 8 * g, K, vec, na);
-        ozt_load8(X, ldx, m0 + r0 + 64, M, k0 + OZT_BK + 8 * g, K, vec, nb);
+      unsigned long long G[8];
+      int neg = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        G[j] = oz_biased<NS>(v[j], emax);
+        neg |= (int)((unsigned long long)__double_as_longlong(v[j]) >> 63) << j;
       }
 #pragma unroll
-      for (int it = 0; it < 2; ++it) {
-        const int r = it ? r0 + 64 : r0;
-        const int emax = it ? e1 : e0;
-        int d[8][NS];
+      for (int p = 1; p <= NS; ++p) {
+        uint32_t w[4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) oz_digits<NS>(it ? vb[j] : va[j], emax, d[j]);
-        const uint32_t off = sw64_offset(r, g);
-#pragma unroll
-        for (int p = 0; p < NS; ++p) {
-          uint32_t w[4];
-#pragma unroll
-          for (int hh = 0; hh < 4; ++hh) {
-            __nv_bfloat162 b2 = __halves2bfloat162(__int2bfloat16_rn(d[2 * hh][p]), __int2bfloat16_rn(d[2 * hh + 1][p]));
-            w[hh] = *(uint32_t*)&b2;
-          }
-          *(uint4*)(xt + p * Cfg::XT + off) = make_uint4(w[0], w[1], w[2], w[3]);
+        for (int hh = 0; hh < 4; ++hh) {
+          int d0 = oz_digit<NS>(G[2 * hh], p), d1 = oz_digit<NS>(G[2 * hh + 1], p);
+          d0 = ((neg >> (2 * hh)) & 1) ? -d0 : d0;
+          d1 = ((neg >> (2 * hh + 1)) & 1) ? -d1 : d1;
+          __nv_bfloat162 b2 = __floats2bfloat162_rn((float)d0, (float)d1);
+          w[hh] = *(uint32_t*)&b2;
         }
+        *(uint4*)(xt + (p - 1) * Cfg::XT + off) = make_uint4(w[0], w[1], w[2], w[3]);
       }
       fence_proxy_async_smem();
       mbar_arrive(&bars[st]);
-      if (c + 1 < nchunk) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) { va[j] = na[j]; vb[j] = nb[j]; }
-      }
     }
     if (!ok) { *abort_s = 1; atomicExch(err, 1); }
     if (t == 0 && *abort_s) {  // let this thread's Y copies land before the CTA exits
@@ -256,14 +248,14 @@ __global__ void __launch_bounds__(OZT_THREADS, 1)
     // ---- epilogue: wait for the last MMAs, combine the levels, write C
     if (ok && mbar_wait(&bars[4], 0, OZT_WAIT, abort_s)) {
       tc_fence_after();
-      const int lg = warp & 3, half = warp >> 2;
-      const int r = 32 * lg + lane;
-      const long long m = m0 + r;
-      const int emax = ex_s[r];
-      const int ex = (emax ? emax - 1022 : 0) - OZ_BETA * (NS + 1);
+      const int lg = warp & 3, quarter = warp >> 2;
+      const int re = 32 * lg + lane;
+      const long long m = m0 + re;
+      const int eme = ex_s[re];
+      const int ex = (eme ? eme - 1022 : 0) - OZ_BETA * (NS + 1);
       const uint32_t trow = tmem + ((uint32_t)(32 * lg) << 16);
 #pragma unroll 1
-      for (int cb = half * (BN / 2); cb < (half + 1) * (BN / 2); cb += 8) {
+      for (int cb = 8 * quarter; cb < BN; cb += 32) {
         float P[NS][8];
 #pragma unroll
         for (int L = 0; L < NS; ++L) tmem_ld8(trow + L * BN + cb, P[L]);

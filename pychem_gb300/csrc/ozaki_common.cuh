@@ -12,11 +12,16 @@ __device__ __forceinline__ unsigned long long oz_absbits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
 
-// The NS signed digits of x for the exponent field emax of its vector's max.
+// The 63-bit fixed-point magnitude F = |x| 2^{63-e} of x for the exponent field emax
+// of its vector's largest |x| (max |x| < 2^e, e = emax - 1022), biased for the signed
+// digit split: G = F + B with B = sum_p 64 * 2^{63 - 7p} + 2^{62 - 7 NS}.  Then
+// u_p = (G >> (63 - 7p)) & 127 (no mask for p = 1) gives the balanced base-128 digits
+// d_p = u_p - 64 of F rounded to nearest at the last digit: the additions of 64 carry
+// exactly as the signed-digit rebalancing would, d_1 in [0, 128], d_p in [-64, 63].
 template <int NS>
-__device__ __forceinline__ void oz_digits(double x, int emax, int* d) {
+__device__ __forceinline__ unsigned long long oz_biased(double x, int emax) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-  const int e = emax ? emax - 1022 : 0;  // max < 2^e
+  const int e = emax ? emax - 1022 : 0;
   const int ex = (int)((u >> 52) & 0x7FF);
   unsigned long long F = 0;
   if (ex != 0 && emax != 0) {
@@ -25,21 +30,27 @@ __device__ __forceinline__ void oz_digits(double x, int emax, int* d) {
     if (sh >= 0) F = mant << sh;
     else if (sh > -64) F = mant >> (-sh);
   }
-  const int lowbit = 63 - OZ_BETA * NS;  // first bit below the last digit
+  unsigned long long B = 1ull << (62 - OZ_BETA * NS);
 #pragma unroll
-  for (int p = 1; p <= NS; ++p) d[p - 1] = (int)((F >> (63 - OZ_BETA * p)) & 127ull);
-  if (lowbit >= 1) d[NS - 1] += (int)((F >> (lowbit - 1)) & 1ull);  // round the last digit
-  int carry = 0;
+  for (int p = 1; p <= NS; ++p) B += 64ull << (63 - OZ_BETA * p);
+  return F + B;
+}
+
+template <int NS>
+__device__ __forceinline__ int oz_digit(unsigned long long G, int p) {  // p = 1 .. NS
+  return p == 1 ? (int)(G >> (63 - OZ_BETA)) - 64 : (int)((G >> (63 - OZ_BETA * p)) & 127ull) - 64;
+}
+
+// The NS signed digits of x for the exponent field emax of its vector's max:
+// x = 2^e sum_p d_p 2^{-7p} + O(2^{e - 7 NS - 1}), |d_1| <= 128, |d_p| <= 64.
+template <int NS>
+__device__ __forceinline__ void oz_digits(double x, int emax, int* d) {
+  const unsigned long long G = oz_biased<NS>(x, emax);
+  const int neg = (int)((unsigned long long)__double_as_longlong(x) >> 63);
 #pragma unroll
-  for (int p = NS - 1; p >= 1; --p) {
-    const int t = d[p] + carry;
-    carry = t >= 64 ? 1 : 0;
-    d[p] = t - 128 * carry;
-  }
-  d[0] += carry;
-  if ((u >> 63) != 0) {
-#pragma unroll
-    for (int p = 0; p < NS; ++p) d[p] = -d[p];
+  for (int p = 1; p <= NS; ++p) {
+    const int v = oz_digit<NS>(G, p);
+    d[p - 1] = neg ? -v : v;
   }
 }
 
