@@ -274,6 +274,29 @@ int pcg_ozaki_gemm_tc(long long M, int N, int K, const double *X, long long ldx,
                       void *workspace, size_t ws_bytes, void *stream);
 int pcg_ozaki_tc_status(const void *workspace, void *stream);
 
+/* Small dense FP64 algebra of the SCF iteration (no upstream counterpart as kernels;
+ * they replace the numpy products of Methods/hartree_fock.py:168-184,226-237 and the
+ * DIIS of Methods/hf_extensions/diis.py:32-41,108-112).
+ * pcg_dgemm: C[b][m][n] = alpha sum_k A[b][m][k] B[b][k][n] + beta C[b][m][n], element
+ *   strides for every axis (transposes by strides); beta = 0 does not read C.
+ * pcg_oa_correction: E (n x n) of one Ogita-Aishima refinement step X <- X + X E from
+ *   S = X^T A X and R = I - X^T X; mode 0 decouples the first nocc columns from the
+ *   rest, mode 1 separates every pair with |lam_j - lam_i| > *delta (a device scalar,
+ *   NULL = 0); lam (optional, n) receives the Rayleigh quotients S_ii / (1 - R_ii).
+ * pcg_diis_step: store F and residual R (len doubles each) in slot state[0] % cap of
+ *   the rings focks / resids (cap x len), add the new row of the residual
+ *   inner-product matrix Bm (cap x cap), solve the C1 system over the slots in use
+ *   (oldest dropped while singular), write the coefficients (cap) and the
+ *   extrapolated Fx (len), and advance state[0].  row: cap doubles of scratch.  No
+ *   host round trip. */
+int pcg_dgemm(int batch, int M, int N, int K, double alpha, const double *A, long long sAb, long long sAm,
+              long long sAk, const double *B, long long sBb, long long sBk, long long sBn, double beta, double *C,
+              long long sCb, long long sCm, long long sCn, void *stream);
+int pcg_oa_correction(int n, int nocc, int mode, const double *delta, const double *S, const double *R, double *E,
+                      double *lam, void *stream);
+int pcg_diis_step(long long len, int cap, int *state, const double *F, const double *R, double *focks,
+                  double *resids, double *Bm, double *row, double *coef, double *Fx, void *stream);
+
 /* Batched symmetric eigensolver (no upstream counterpart; replaces the LAPACK eigh of
  * Methods/hartree_fock.py:172-175,226): parallel cyclic Jacobi, one CTA per matrix.
  * A: batch x n x n FP64 (read only); w: batch x n eigenvalues (unsorted, matching the
