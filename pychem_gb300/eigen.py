@@ -1,21 +1,23 @@
 """Symmetric eigensolver for the SCF on the GPU (replaces numpy.linalg.eigh of
-``Methods/hartree_fock.py:172-175,226``).
+``Methods/hartree_fock.py:172-175,226``), on the library's own kernels only:
 
 * n <= 136: parallel cyclic Jacobi in FP64, one CTA per matrix (pcg_jacobi_eigh),
   batched over any leading dimension.
-* larger n, inside SCF iterations: FP64 iterative refinement of the previous
-  iteration's eigenvectors (T. Ogita and K. Aishima, "Iterative refinement for
+* larger n: the FP32 variant of the Jacobi kernel (FP32-accurate vectors, n <= 334),
+  then FP64 iterative refinement (T. Ogita and K. Aishima, "Iterative refinement for
   symmetric eigenvalue decomposition", Japan J. Indust. Appl. Math. 35 (2018)
-  1007-1035, Algorithm 1): four FP64 GEMMs per step instead of a tridiagonalisation.
-* the FP32 variant of the Jacobi kernel (``jacobi(..., fp32=True)``) gives FP32-accurate
-  starting vectors for the same refinement.
+  1007-1035, Algorithm 1) with the library's FP64 GEMM (pcg_dgemm) and correction
+  kernel (pcg_oa_correction).  Inside SCF iterations the refinement starts from the
+  previous iteration's vectors and only decouples the occupied columns; exact
+  solutions slice the spectrum at gaps into parts of at most 136, which the FP64
+  Jacobi kernel finishes, so near-degenerate clusters are resolved exactly.
 Eigenvalues are returned ascending with matching eigenvector columns.
 """
 import ctypes
 
 import torch
 
-from . import _lib
+from . import _lib, dense
 
 FP64_JACOBI_MAX_N = 136
 
@@ -47,6 +49,19 @@ def eigh32(A, X_prev=None):
     return _sort(*_jacobi(A.to(torch.float64), True, 40, None))
 
 
+def eigh32_own(A, X_prev=None):
+    """eigh32 for one matrix (n, n) with FP64 in and out and the library GEMM for the
+    rotations into and out of X_prev's basis: FP32-accurate eigenpairs, ascending."""
+    A = A.to(torch.float64)
+    if X_prev is not None:
+        Xp = X_prev.to(torch.float64)
+        Ap = dense.mm(Xp, dense.mm(A, Xp), ta=True)
+        w, V = _jacobi(Ap, True, 40, None)
+        return _sort(w, dense.mm(Xp, V.to(torch.float64)))
+    w, V = _jacobi(A, True, 40, None)
+    return _sort(w, V.to(torch.float64))
+
+
 def _jacobi(A, fp32, max_sweeps, tol):
     shape = A.shape
     n = shape[-1]
@@ -69,101 +84,138 @@ def _sort(w, V):
     return w, V
 
 
+def _rs(A, X):
+    """R = I - X^T X and S = X^T A X on the library GEMM."""
+    n = X.shape[-1]
+    R = torch.eye(n, dtype=torch.float64, device=X.device)
+    dense.mm(X, X, ta=True, out=R, alpha=-1.0, beta=1.0)
+    S = dense.mm(X, dense.mm(A, X), ta=True)
+    return R, S
+
+
+def _step(X, E):
+    Xn = X.clone()
+    return dense.mm(X, E, out=Xn, beta=1.0)
+
+
 def refine(A, X, steps=2):
     """Ogita-Aishima refinement of approximate eigenvectors X of symmetric A (FP64).
     Pairs with |l_i - l_j| <= delta, delta = 2 (||S - diag(l)||_F + ||A||_F ||R||_F) (the
-    paper's 2-norms bounded by Frobenius norms), are only re-orthogonalised: from an
-    FP32 start, vectors inside a cluster of near-degenerate eigenvalues stay mixed
-    within the cluster while everything separated by more than delta converges
-    quadratically.  The SCF needs only the occupied-space projector, which a mixed
-    occupied (or virtual) cluster leaves unchanged."""
-    n = A.shape[-1]
-    I = torch.eye(n, dtype=torch.float64, device=A.device)
-    lam = None
+    paper's 2-norms bounded by Frobenius norms), are only re-orthogonalised: vectors
+    inside a cluster of near-degenerate eigenvalues stay mixed within the cluster
+    while everything separated by more than delta converges quadratically.  Batched
+    over a leading dimension; no host round trip."""
+    if X.dim() == 3:
+        out = [refine(A[k] if A.dim() == 3 else A, X[k], steps) for k in range(X.shape[0])]
+        return torch.stack([o[0] for o in out]), torch.stack([o[1] for o in out])
+    X = X.to(torch.float64)
+    lam = torch.empty(X.shape[-1], dtype=torch.float64, device=X.device)
+    nA = torch.linalg.vector_norm(A)
     for _ in range(steps):
-        R = I - X.transpose(-1, -2) @ X
-        S = X.transpose(-1, -2) @ (A @ X)
-        lam = torch.diagonal(S, dim1=-2, dim2=-1) / (1.0 - torch.diagonal(R, dim1=-2, dim2=-1))
-        off = S - torch.diag_embed(lam)
-        nA = A.flatten(-2).norm(dim=-1)
-        delta = 2.0 * (off.flatten(-2).norm(dim=-1) + nA * R.flatten(-2).norm(dim=-1))
-        dl = lam.unsqueeze(-2) - lam.unsqueeze(-1)          # [i, j] = lam_j - lam_i
-        sep = dl.abs() > delta.unsqueeze(-1).unsqueeze(-1)
-        E = torch.where(sep, (S + lam.unsqueeze(-2) * R) / torch.where(sep, dl, torch.ones_like(dl)), 0.5 * R)
-        X = X + X @ E
-    return lam, X
+        R, S = _rs(A, X)
+        l = torch.diagonal(S) / (1.0 - torch.diagonal(R))
+        delta = 2.0 * (torch.linalg.vector_norm(S - torch.diag(l)) + nA * torch.linalg.vector_norm(R))
+        E = dense.oa_correction(S, R, 0, 1, delta=delta, lam=lam)
+        X = _step(X, E)
+    return lam.clone(), X
 
 
-def refine_projector(A, X, nocc, steps=2):
+def refine_projector(A, X, nocc, steps=2, check=False):
     """Refinement that only decouples the first nocc columns (occupied) from the rest
     (virtual): Ogita-Aishima corrections for occupied-virtual pairs, separated by at
     least the HOMO-LUMO gap, and re-orthonormalisation (E = R/2) inside each block.
     Converges quadratically in the occupied-space projector regardless of
-    near-degeneracies inside the blocks."""
-    n = A.shape[-1]
-    I = torch.eye(n, dtype=torch.float64, device=A.device)
-    occ = torch.zeros(n, dtype=torch.bool, device=A.device)
-    occ[:nocc] = True
-    ov = occ.unsqueeze(-1) ^ occ.unsqueeze(-2)
-    lam = None
+    near-degeneracies inside the blocks.  With check=True also returns a device
+    vector (orthogonality error, largest occupied-virtual coupling, minus the gap
+    between the blocks' Rayleigh quotients) of the refined vectors."""
+    lam = torch.empty(X.shape[-1], dtype=torch.float64, device=X.device)
     for _ in range(steps):
-        R = I - X.transpose(-1, -2) @ X
-        S = X.transpose(-1, -2) @ (A @ X)
-        lam = torch.diagonal(S) / (1.0 - torch.diagonal(R))
-        dl = lam.unsqueeze(-2) - lam.unsqueeze(-1)
-        E = torch.where(ov, (S + lam.unsqueeze(-2) * R) / torch.where(ov, dl, torch.ones_like(dl)), 0.5 * R)
-        X = X + X @ E
-    return lam, X
+        R, S = _rs(A, X)
+        E = dense.oa_correction(S, R, nocc, 0, lam=lam)
+        X = _step(X, E)
+    if not check:
+        return lam, X
+    R, S = _rs(A, X)
+    d = torch.diagonal(S)
+    chk = torch.stack([R.abs().amax(), S[:nocc, nocc:].abs().amax(), d[:nocc].amax() - d[nocc:].amin()])
+    return lam, X, chk
+
+
+def _split_point(w, n):
+    """Where to slice an ascending spectrum of size n > 136: the largest gap among the
+    positions that leave both parts at most 136 long (the middle third when none do)."""
+    lo, hi = max(1, n - FP64_JACOBI_MAX_N), min(n - 1, FP64_JACOBI_MAX_N)
+    if lo > hi:
+        lo, hi = n // 3, (2 * n) // 3
+    gaps = w[lo:hi + 1] - w[lo - 1:hi]
+    return lo + int(torch.argmax(gaps))
+
+
+def exact_eigh(A, X_prev=None, steps=4):
+    """Eigenpairs of one symmetric A to FP64 accuracy on the library's kernels, by
+    spectrum slicing: n <= 136, the FP64 Jacobi kernel started from the FP32 Jacobi
+    vectors (so it needs few sweeps); larger n, the FP32 Jacobi vectors (from X_prev
+    when given), a split at the largest gap that keeps both parts small, projector
+    refinement that decouples the two invariant subspaces in FP64, and the same on
+    each part's projected matrix.  Near-degenerate clusters end up inside one part,
+    where Jacobi resolves them."""
+    n = A.shape[-1]
+    if n <= FP64_JACOBI_MAX_N:
+        _, V32 = eigh32_own(A, X_prev)
+        Ap = dense.mm(V32, dense.mm(A, V32), ta=True)
+        w, U = jacobi(0.5 * (Ap + Ap.T))
+        return _sort(w, dense.mm(V32, U))
+    w32, V = eigh32_own(A, X_prev)
+    s = _split_point(w32, n)
+    _, V = refine_projector(A, V, s, steps=steps)
+    out_w, out_V = [], []
+    for blk in (V[:, :s], V[:, s:]):
+        Ab = dense.mm(blk, dense.mm(A, blk), ta=True)
+        wb, Ub = exact_eigh(0.5 * (Ab + Ab.T))
+        out_w.append(wb)
+        out_V.append(dense.mm(blk, Ub))
+    return _sort(torch.cat(out_w), torch.cat(out_V, dim=1))
 
 
 def eigh(A, X_prev=None, refine_steps=2, exact=True, check_tol=1e-10, nocc=None):
     """Ascending eigenvalues and eigenvectors of symmetric FP64 A (..., n, n).
 
     n <= 136: batched FP64 Jacobi (exact to rounding; the small-molecule ensemble).
-    Larger n, exact=False and a previous eigenvector matrix X_prev (consecutive SCF
-    iterations): FP64 refinement starting from X_prev -- quadratic convergence for
-    every pair separated by more than the refinement threshold; pairs inside a
-    near-degenerate cluster may stay rotated within it, which leaves the occupied-
-    space projector unchanged.  The result is checked (orthogonality and the
-    residual of separated pairs); on failure, and whenever exact=True or there is no
-    X_prev, the library solver (cuSOLVER) is used."""
+    Larger n (one matrix): exact=True or no X_prev -- spectrum slicing (exact_eigh);
+    otherwise refinement from X_prev (consecutive SCF iterations): with nocc, only the
+    occupied-space projector is converged (checked: orthonormal, decoupled, gapped;
+    else the exact route); without nocc, full refinement (checked for orthogonality,
+    else the exact route)."""
     n = A.shape[-1]
     if n <= FP64_JACOBI_MAX_N:
         if X_prev is not None:
-            Ap = X_prev.transpose(-1, -2) @ A @ X_prev
+            shape = A.shape
+            A3, X3 = A.reshape(-1, n, n), X_prev.reshape(-1, n, n)
+            if A3.shape[0] == 1:
+                A3, X3 = A3[0], X3[0]
+            Ap = dense.mm(X3, dense.mm(A3, X3), ta=True)
             w, V = jacobi(Ap)
-            return _sort(w, X_prev @ V)
+            return _sort(w.reshape(shape[:-1]), dense.mm(X3, V).reshape(shape))
         return _sort(*jacobi(A))
     if exact or X_prev is None:
         stats["exact"] += 1
-        return torch.linalg.eigh(A)
-    I = torch.eye(n, dtype=torch.float64, device=A.device)
+        return exact_eigh(A, X_prev)
     if nocc is not None:
-        # SCF iterations: only the occupied-space projector matters.  Refine in rounds
-        # of refine_steps steps until the vectors are orthonormal, the occupied block is
-        # decoupled (max |(X^T A X)_ov| <= check_tol |A|) and gapped; after three rounds
-        # fall back to the exact solver.
+        scale = max(float(A.abs().amax()), 1.0)
         X = X_prev
-        scale = float(A.abs().amax())
-        ok = False
         for _ in range(3):
-            w, X = refine_projector(A, X, nocc, steps=refine_steps)
-            orth = (X.transpose(-1, -2) @ X - I).abs().amax()
-            ov = (X[:, :nocc].transpose(-1, -2) @ (A @ X[:, nocc:])).abs().amax()
-            gap = w[nocc:].min() - w[:nocc].max()
-            chk = torch.stack([orth, ov, -gap]).cpu()
-            if float(chk[0]) <= check_tol and float(chk[1]) <= check_tol * max(scale, 1.0) and float(chk[2]) < 0.0:
-                ok = True
-                break
-        if not ok:
-            stats["fallback"] += 1
-            return torch.linalg.eigh(A)
-        stats["refined"] += 1
-        wo, io = torch.sort(w[:nocc])
-        wv, iv = torch.sort(w[nocc:])
-        return torch.cat([wo, wv]), torch.cat([X[:, :nocc][:, io], X[:, nocc:][:, iv]], dim=1)
+            w, X, chk = refine_projector(A, X, nocc, steps=refine_steps, check=True)
+            c = chk.cpu()
+            if float(c[0]) <= check_tol and float(c[1]) <= check_tol * scale and float(c[2]) < 0.0:
+                stats["refined"] += 1
+                wo, io = torch.sort(w[:nocc])
+                wv, iv = torch.sort(w[nocc:])
+                return torch.cat([wo, wv]), torch.cat([X[:, :nocc][:, io], X[:, nocc:][:, iv]], dim=1)
+        stats["fallback"] += 1
+        return exact_eigh(A, X_prev)
     w, X = refine(A, X_prev, steps=refine_steps)
-    orth = (X.transpose(-1, -2) @ X - I).abs().amax()
-    if float(orth) > check_tol:
-        return torch.linalg.eigh(A)
+    R, _ = _rs(A, X)
+    if float(R.abs().amax()) > check_tol:
+        stats["fallback"] += 1
+        return exact_eigh(A, X_prev)
     return _sort(w, X)

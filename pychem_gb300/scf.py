@@ -33,24 +33,24 @@ LINEAR_DEPENDENCE = 1.0e-6   # Data/constants.py:34
 
 def orthogonaliser(S, canonical=False):
     """X with X^T S X = I.  Upstream (hartree_fock.py:226-237) uses the canonical
-    U s^-1/2 with eigenvalues s <= 1e-6 dropped.  Unless canonical=True, a Cholesky
-    factor is used instead, X = L^-T, when the smallest eigenvalue of S (estimated by
-    power iteration on S^-1 = L^-T L^-1) is above 1e-5: then nothing would be dropped
-    and energies and orbitals do not depend on the choice of X; otherwise the canonical
-    route."""
-    if not canonical and S.shape[0] > eigen.FP64_JACOBI_MAX_N:
-        L, info = torch.linalg.cholesky_ex(S)
-        if int(info) == 0:
-            n = S.shape[0]
-            Li = torch.linalg.solve_triangular(L, torch.eye(n, dtype=S.dtype, device=S.device), upper=False)
-            v = torch.ones(n, dtype=S.dtype, device=S.device) / math.sqrt(n)
-            mu = torch.zeros((), dtype=S.dtype, device=S.device)
-            for _ in range(12):
-                w = Li.T @ (Li @ v)
-                mu = torch.linalg.vector_norm(w)
+    U s^-1/2 with eigenvalues s <= 1e-6 dropped.  For n > 136, unless canonical=True,
+    the symmetric X = S^-1/2 from the coupled Newton-Schulz iteration (library GEMMs
+    only) is used when the smallest eigenvalue of S, estimated by power iteration on
+    X^2 = S^-1, is above 1e-5: then nothing would be dropped and energies and orbitals
+    do not depend on the choice of X; otherwise the canonical route."""
+    from . import dense
+    n = S.shape[0]
+    if not canonical and n > eigen.FP64_JACOBI_MAX_N:
+        X, ok = dense.inv_sqrt(S)
+        if ok:
+            v = torch.ones(n, 1, dtype=S.dtype, device=S.device) / math.sqrt(n)
+            mu = 1.0
+            for _ in range(16):
+                w = dense.mm(X, dense.mm(X, v))
+                mu = float(torch.linalg.vector_norm(w))
                 v = w / mu
-            if 1.0 / float(mu) > 10.0 * LINEAR_DEPENDENCE:
-                return Li.T.contiguous()
+            if 1.0 / mu > 10.0 * LINEAR_DEPENDENCE:
+                return X
     s, U = eigen.eigh(S, exact=True)
     s = torch.flip(s, [0])
     U = torch.flip(U, [1])
@@ -94,16 +94,23 @@ class SCFResult(dict):
 
 
 def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=1, D0=None, record=False,
-        guess="sad", exact_iters=3):
+        guess="sad", exact_iters=1, graph=None):
     """Restricted Hartree-Fock on a prepared GpuEngine.  Returns SCFResult with
     E (total), E_elec, C, eps, D (alpha density), iterations, converged.
     guess: "sad" (superposition of atomic densities, default), "core" (upstream's
     core-Hamiltonian guess), or an explicit alpha density D0.
 
     Fock matrices are kept in the orthonormal basis, F' = X^T F X; the DIIS residual
-    is D'F' - F'D' (= X^T (S D F - F D S) X for D = X D' X^T) and DIIS extrapolates F'.
-    The first exact_iters iterations diagonalise exactly; later ones refine the
-    previous eigenvectors (checked, with fallback to the exact solver)."""
+    is D'F' - F'D' (= X^T (S D F - F D S) X for D = X D' X^T) and DIIS extrapolates F'
+    with its Pulay system solved on the GPU.  Every step runs on the library's
+    kernels: Fock digestion, FP64 GEMMs (pcg_dgemm), the eigenvectors (Jacobi for the
+    first exact_iters iterations, then refinement of the previous vectors that
+    decouples the occupied space, checked, with the Jacobi route when the check
+    fails), the density C_occ C_occ^T on the tensor cores (pcg_ozaki_gemm_tc).  For
+    n > 136 (graph None or True) every iteration after the first exact_iters is one
+    CUDA graph replay followed by one read of five numbers (energy, density change,
+    refinement checks)."""
+    from . import dense
     mol = engine.mol
     nocc = mol.NAlphaElectrons
     if mol.NAlphaElectrons != mol.NBetaElectrons:
@@ -111,51 +118,109 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
     S, H = engine.S, engine.H
     dev = S.device
     e_nuc = mol.nuclear_repulsion()
+    n = engine.nbf
+    big = n > eigen.FP64_JACOBI_MAX_N
+    use_graph = big if graph is None else (graph and big)
     X = orthogonaliser(S)
-    Xt = X.T.contiguous()
-    state = {"Q": None}
+    n2 = X.shape[1]
+    mm = dense.mm
 
-    def diagonalise(Fp, exact=False):
-        e, Q = eigen.eigh(Fp, X_prev=state["Q"], refine_steps=2, exact=exact, nocc=nocc)
-        state["Q"] = Q
-        return e, X @ Q
-
+    # static buffers (the CUDA graph reads and writes these addresses)
+    D = torch.empty(n, n, dtype=torch.float64, device=dev)
     if D0 is not None:
-        D = D0.clone()
+        D.copy_(D0)
     elif guess == "sad":
         from .guess import sad_density
-        D = sad_density(mol, device=dev)
+        D.copy_(sad_density(mol, device=dev))
     else:
-        eps, C = diagonalise(Xt @ H @ X)
-        D = C[:, :nocc] @ C[:, :nocc].T
-    Dp = Xt @ S @ D @ S @ X      # orthonormal-basis density
-    n = engine.nbf
+        _, Q0 = eigen.eigh(mm(X, mm(H, X), ta=True), exact=True)
+        C0 = mm(X, Q0)
+        mm(C0[:, :nocc], C0[:, :nocc], tb=True, out=D)
+    Dp = mm(X, mm(mm(S, D), mm(S, X)), ta=True)      # orthonormal-basis density
     F = torch.empty(n, n, dtype=torch.float64, device=dev)
     G = torch.empty(n, n, dtype=torch.float64, device=dev)
-    focks, resids = [], []
-    Bmat = np.zeros((0, 0))
-    E_old = D_old = None
+    Fp = torch.empty(n2, n2, dtype=torch.float64, device=dev)
+    R = torch.empty(n2, n2, dtype=torch.float64, device=dev)
+    Fx = torch.empty(n2, n2, dtype=torch.float64, device=dev)
+    Q = torch.eye(n2, dtype=torch.float64, device=dev)
+    C = torch.empty(n, n2, dtype=torch.float64, device=dev)
+    Dold = torch.zeros(n, n, dtype=torch.float64, device=dev)
+    vals = torch.zeros(5, dtype=torch.float64, device=dev)
+    diis = dense.DeviceDIIS((n2, n2), diis_size, dev)
+    have_q = [False]
+
+    def fock_and_diis(use_diis):
+        engine.fock(D, out=F, G=G)
+        mm(X, mm(F, X), ta=True, out=Fp)
+        P = mm(Dp, Fp)
+        torch.sub(P, P.T, out=R)
+        vals[0] = torch.sum(D * (H + F))
+        vals[1] = torch.sqrt(torch.mean((D - Dold) ** 2))
+        Dold.copy_(D)
+        if use_diis:
+            diis.step(Fp, R, Fx)
+        else:
+            Fx.copy_(Fp)
+
+    def density():
+        mm(X, Q, out=C)
+        if big:
+            ozaki_gemm_tc(C, C, D, n, n, nocc, n2, (1, n2), (n, 1))      # D = C_occ C_occ^T
+        else:
+            mm(C[:, :nocc], C[:, :nocc], tb=True, out=D)
+        mm(Q[:, :nocc], Q[:, :nocc], tb=True, out=Dp)
+
+    def diag_exact():
+        if big:
+            _, V = eigen.eigh32_own(Fx, Q if have_q[0] else None)
+            _, V = eigen.refine_projector(Fx, V, nocc, steps=2)
+        else:
+            _, V = eigen.eigh(Fx, X_prev=Q if have_q[0] else None)
+        Q.copy_(V)
+        have_q[0] = True
+        vals[2:] = 0.0
+
+    def diag_refine():
+        _, V, chk = eigen.refine_projector(Fx, Q, nocc, steps=2, check=True)
+        Q.copy_(V)
+        vals[2:] = chk
+
+    g = None
+    per_replay = 0
+    E_old = None
     history = []
     converged = False
     it = 0
+    scale = None
     for it in range(1, max_iter + 1):
-        engine.fock(D, out=F, G=G)
-        use_diis = it > diis_start
-        Fp = Xt @ F @ X
-        if use_diis:
-            P = Dp @ Fp
-            R = P - P.T
+        exact = it <= exact_iters or not big
+        if exact or not use_graph:
+            fock_and_diis(it > diis_start)
+            if exact:
+                diag_exact()
+            else:
+                diag_refine()
+            density()
         else:
-            R = None
-        # one device->host read per iteration: energy, density change, new DIIS row
-        vals = [torch.sum(D * (H + F)).reshape(1)]
-        vals.append(torch.sqrt(torch.mean((D - D_old) ** 2)).reshape(1) if D_old is not None
-                    else torch.zeros(1, dtype=torch.float64, device=dev))
-        if use_diis:
-            rv = R.reshape(-1)
-            vals.append(torch.stack([torch.dot(rv, r.reshape(-1)) for r in resids] + [torch.dot(rv, rv)]))
-        host = torch.cat(vals).cpu().numpy()
+            if g is None:
+                torch.cuda.synchronize()
+                g = torch.cuda.CUDAGraph()
+                c0 = _lib_launches()
+                with torch.cuda.graph(g):
+                    fock_and_diis(True)
+                    diag_refine()
+                    density()
+                per_replay = _lib_launches() - c0
+            g.replay()
+            _lib_add_launches(per_replay)
+        host = vals.cpu().numpy()
         E = float(host[0]) + e_nuc
+        if not exact:
+            if scale is None:
+                scale = max(float(Fx.abs().amax()), 1.0)
+            if not (host[2] <= 1e-10 and host[3] <= 1e-10 * scale and host[4] < 0.0):
+                diag_exact()                    # refinement did not converge: Jacobi route, then continue
+                density()
         if E_old is not None:
             drms = float(host[1])
             dE = E - E_old
@@ -164,36 +229,37 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
             if abs(dE) < e_tol and drms < d_tol:
                 converged = True
                 break
-        E_old, D_old = E, D
-        Fx = Fp
-        if use_diis:
-            row = host[2:]
-            m = len(resids) + 1
-            Bn = np.zeros((m, m))
-            Bn[:m - 1, :m - 1] = Bmat
-            Bn[m - 1, :] = row
-            Bn[:, m - 1] = row
-            focks.append(Fp)
-            resids.append(R)
-            Bmat = Bn
-            if len(focks) > diis_size:
-                focks.pop(0); resids.pop(0)
-                Bmat = Bmat[1:, 1:]
-            if len(focks) > 1:
-                c = diis_coefficients(Bmat)
-                cw = torch.tensor(c, dtype=torch.float64, device=dev)
-                Fx = torch.einsum("k,kij->ij", cw, torch.stack(focks))
-        eps, C = diagonalise(Fx, exact=it <= exact_iters)
-        Co = C[:, :nocc]
-        D = Co @ Co.T
-        Qo = state["Q"][:, :nocc]
-        Dp = Qo @ Qo.T
+        E_old = E
     # orbitals of the final Fock matrix, exact (including inside near-degenerate
-    # clusters) for MP2's denominators; the refined vectors of the last iterations are
-    # converged only as an occupied/virtual split
-    eps, C = diagonalise(Xt @ F @ X, exact=True)
-    return SCFResult(E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=C, eps=eps, D=D, F=F, iterations=it,
+    # clusters) for MP2's denominators: for n > 136 the occupied and virtual blocks of
+    # the refined vectors are decoupled once more and each block is diagonalised
+    # exactly (spectrum slicing inside blocks above 136)
+    Ff = mm(X, mm(F, X), ta=True)
+    if big:
+        _, V = eigen.refine_projector(Ff, Q, nocc, steps=2)
+        ws, Vs = [], []
+        for blk in (V[:, :nocc], V[:, nocc:]):
+            Ab = mm(blk, mm(Ff, blk), ta=True)
+            wb, Ub = eigen.exact_eigh(0.5 * (Ab + Ab.T))
+            ws.append(wb)
+            Vs.append(mm(blk, Ub))
+        eps, Qf = torch.cat(ws), torch.cat(Vs, dim=1)
+    else:
+        eps, Qf = eigen.eigh(Ff, exact=True)
+    Cf = mm(X, Qf)
+    Dn = mm(Cf[:, :nocc], Cf[:, :nocc], tb=True)
+    return SCFResult(E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=Cf, eps=eps, D=Dn, F=F, iterations=it,
                      converged=converged, history=history, fock_builds=it)
+
+
+def _lib_launches():
+    from . import _lib
+    return _lib.launch_count
+
+
+def _lib_add_launches(k):
+    from . import _lib
+    _lib.launch_count += k
 
 
 _TC_WS = {}
