@@ -282,7 +282,8 @@ int pcg_ozaki_tc_status(const void *workspace, void *stream);
  * pcg_oa_correction: E (n x n) of one Ogita-Aishima refinement step X <- X + X E from
  *   S = X^T A X and R = I - X^T X; mode 0 decouples the first nocc columns from the
  *   rest, mode 1 separates every pair with |lam_j - lam_i| > *delta (a device scalar,
- *   NULL = 0); lam (optional, n) receives the Rayleigh quotients S_ii / (1 - R_ii).
+ *   NULL = 0); lam (optional, n) receives the Rayleigh quotients
+ *   S_ii / (1 - R_ii).
  * pcg_diis_step: store F and residual R (len doubles each) in slot state[0] % cap of
  *   the rings focks / resids (cap x len), add the new row of the residual
  *   inner-product matrix Bm (cap x cap), solve the C1 system over the slots in use

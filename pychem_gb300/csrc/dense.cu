@@ -81,8 +81,9 @@ __global__ void k_oa_correction(int n, int nocc, int mode, const double* __restr
   const double lj = __ldg(S + (long long)j * n + j) / (1.0 - __ldg(R + (long long)j * n + j));
   const double dl = lj - li;
   const double delta = delta_p ? *delta_p : 0.0;
+  const double num = __ldg(S + idx) + lj * __ldg(R + idx);
   const bool sep = mode == 0 ? ((i < nocc) != (j < nocc)) : (fabs(dl) > delta);
-  E[idx] = sep ? (__ldg(S + idx) + lj * __ldg(R + idx)) / dl : 0.5 * __ldg(R + idx);
+  E[idx] = sep ? num / dl : 0.5 * __ldg(R + idx);
   if (lam_out && j == 0) lam_out[i] = li;
 }
 

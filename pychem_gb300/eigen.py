@@ -49,17 +49,29 @@ def eigh32(A, X_prev=None):
     return _sort(*_jacobi(A.to(torch.float64), True, 40, None))
 
 
-def eigh32_own(A, X_prev=None):
+def eigh32_own(A, X_prev=None, tol=1e-5, max_sweeps=12):
     """eigh32 for one matrix (n, n) with FP64 in and out and the library GEMM for the
-    rotations into and out of X_prev's basis: FP32-accurate eigenpairs, ascending."""
+    rotations into and out of X_prev's basis: FP32-accurate eigenpairs, ascending.
+    The Jacobi sweeps stop at an off-diagonal norm of tol (relative): the result
+    only seeds FP64 refinement, which needs vectors good to well inside the gaps it
+    separates, not FP32's last digit."""
     A = A.to(torch.float64)
     if X_prev is not None:
         Xp = X_prev.to(torch.float64)
         Ap = dense.mm(Xp, dense.mm(A, Xp), ta=True)
-        w, V = _jacobi(Ap, True, 40, None)
+        w, V = _jacobi(Ap, True, max_sweeps, tol)
         return _sort(w, dense.mm(Xp, V.to(torch.float64)))
-    w, V = _jacobi(A, True, 40, None)
+    w, V = _jacobi(A, True, max_sweeps, tol)
     return _sort(w, V.to(torch.float64))
+
+
+def orthonormalize(X, steps=2):
+    """X <- X + X (I - X^T X) / 2, twice: columns orthonormal to FP64 rounding from
+    FP32-orthonormal ones (Newton-Schulz for the polar factor)."""
+    for _ in range(steps):
+        R, _ = _rs(None, X, need_s=False)
+        X = _step(X, 0.5 * R)
+    return X
 
 
 def _jacobi(A, fp32, max_sweeps, tol):
@@ -84,12 +96,12 @@ def _sort(w, V):
     return w, V
 
 
-def _rs(A, X):
+def _rs(A, X, need_s=True):
     """R = I - X^T X and S = X^T A X on the library GEMM."""
     n = X.shape[-1]
     R = torch.eye(n, dtype=torch.float64, device=X.device)
     dense.mm(X, X, ta=True, out=R, alpha=-1.0, beta=1.0)
-    S = dense.mm(X, dense.mm(A, X), ta=True)
+    S = dense.mm(X, dense.mm(A, X), ta=True) if need_s else None
     return R, S
 
 
@@ -123,9 +135,11 @@ def refine(A, X, steps=2):
 def refine_projector(A, X, nocc, steps=2, check=False):
     """Refinement that only decouples the first nocc columns (occupied) from the rest
     (virtual): Ogita-Aishima corrections for occupied-virtual pairs, separated by at
-    least the HOMO-LUMO gap, and re-orthonormalisation (E = R/2) inside each block.
-    Converges quadratically in the occupied-space projector regardless of
-    near-degeneracies inside the blocks.  With check=True also returns a device
+    least the HOMO-LUMO gap, and re-orthonormalisation (E = R/2) inside each block, so
+    the columns stay orthonormal to rounding.  Quadratic in the occupied-space
+    projector while the blocks of X^T A X are nearly diagonal (X close to
+    eigenvectors); as they drift from diagonal between SCF iterations it becomes a
+    fast linear iteration.  With check=True also returns a device
     vector (orthogonality error, largest occupied-virtual coupling, minus the gap
     between the blocks' Rayleigh quotients) of the refined vectors."""
     lam = torch.empty(X.shape[-1], dtype=torch.float64, device=X.device)
@@ -162,9 +176,10 @@ def exact_eigh(A, X_prev=None, steps=4):
     n = A.shape[-1]
     if n <= FP64_JACOBI_MAX_N:
         _, V32 = eigh32_own(A, X_prev)
-        Ap = dense.mm(V32, dense.mm(A, V32), ta=True)
+        V = orthonormalize(V32)
+        Ap = dense.mm(V, dense.mm(A, V), ta=True)
         w, U = jacobi(0.5 * (Ap + Ap.T))
-        return _sort(w, dense.mm(V32, U))
+        return _sort(w, dense.mm(V, U))
     w32, V = eigh32_own(A, X_prev)
     s = _split_point(w32, n)
     _, V = refine_projector(A, V, s, steps=steps)
@@ -213,9 +228,14 @@ def eigh(A, X_prev=None, refine_steps=2, exact=True, check_tol=1e-10, nocc=None)
                 return torch.cat([wo, wv]), torch.cat([X[:, :nocc][:, io], X[:, nocc:][:, iv]], dim=1)
         stats["fallback"] += 1
         return exact_eigh(A, X_prev)
-    w, X = refine(A, X_prev, steps=refine_steps)
-    R, _ = _rs(A, X)
-    if float(R.abs().amax()) > check_tol:
+    w, X = refine(A, X_prev, steps=refine_steps + 1)
+    # converged when the next correction is negligible: separated pairs' quotients and
+    # the orthogonality terms R/2 both below check_tol
+    R, S = _rs(A, X)
+    l = torch.diagonal(S) / (1.0 - torch.diagonal(R))
+    delta = 2.0 * (torch.linalg.vector_norm(S - torch.diag(l)) + torch.linalg.vector_norm(A) * torch.linalg.vector_norm(R))
+    E = dense.oa_correction(S, R, 0, 1, delta=delta)
+    if float(E.abs().amax()) > check_tol:
         stats["fallback"] += 1
         return exact_eigh(A, X_prev)
     return _sort(w, X)
