@@ -602,6 +602,30 @@ def gpu_arm(args):
         torch.cuda.synchronize()
         e2e_t.append(time.perf_counter() - t0)
     t_e2e = statistics.mean(e2e_t)
+    # the dominant kernel: the four tensor-core Ozaki launches of the MP2 transform,
+    # timed one by one on the launching stream; algorithmic work = the BF16 tensor
+    # flops of the digit-slice products, 2 M N Kp per product, 21 products (6 slices,
+    # levels up to 7), Kp = K rounded up to the 32-column chunk
+    from pychem_gb300.scf import mp2_transform, ozaki_tc_status
+    Ep = eng.dense_eri_pairs()
+    tc_t, tc_flops = 0.0, 0.0
+    tc_runs = []
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        tl = []
+        mp2_transform(Ep, r.C[:, :o].contiguous(), r.C[:, o:].contiguous(), timings=tl)
+        torch.cuda.synchronize()
+        tc_runs.append(tl)
+    tl = tc_runs[-1]
+    for (M_, N_, K_, ev) in tl:
+        kp = (K_ + 31) // 32 * 32
+        ncols = (N_ + 63) // 64 * 64 if N_ > 80 else N_
+        tc_flops += 21 * 2.0 * M_ * ncols * kp
+        tc_t += ev[0].elapsed_time(ev[1]) / 1e3
+    tc_status = ozaki_tc_status("cuda")
+    tc_bytes = sum(M_ * K_ * 8 + M_ * N_ * 8 for (M_, N_, K_, _) in tl)
+    del Ep
     # cross-check of the tensor-core MP2 transform against cuBLAS DGEMM (untimed)
     e2_fp64 = rmp2(eng, r.C, r.eps, gemm="fp64")
     torch.cuda.synchronize()
@@ -650,7 +674,8 @@ def gpu_arm(args):
         "eri_quartets_per_s": quartets / t_eri,
         "fock_builds_per_s": 1.0 / t_fock,
         "mp2_tflops": mp2_flops(n, o, n - o) / ph[3] / 1e12,
-        "mp2": {"gemm": "BF16 tensor cores, Ozaki split, 6 slices", "s": ph[3],
+        "mp2": {"gemm": "tcgen05 BF16 tensor cores, Ozaki digit slices (6), all levels in one kernel (pcg_ozaki_gemm_tc)",
+                "s": ph[3], "tc_launches_s": tc_t, "tc_error_flag": tc_status,
                 "dE_vs_fp64_dgemm": e2 - e2_fp64, "fp64_dgemm_s": t_mp2_fp64,
                 "fp64_dgemm_tflops": mp2_flops(n, o, n - o) / t_mp2_fp64 / 1e12},
         "phases_s": {"setup_1e_schwarz_tasks": ph[0], "eri": ph[1], "scf": ph[2], "mp2": ph[3]},
@@ -658,10 +683,17 @@ def gpu_arm(args):
                   "quartets_fp32": engm.stats["quartets_fp32"], "quartets_fp64": engm.stats["quartets_fp64"],
                   "dE_rhf_vs_fp64": rm.E - r.E, "dE_mp2_vs_fp64": (rm.E + e2m) - (r.E + e2),
                   "eri_s": statistics.mean(p[1] for p in phases_m)},
-        "roofline": {"bound": "fp64", "kernel": "ERI class kernels k_eri<*> (FP64 pipe)",
-                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                     "peak_source": "measured by bench.py FP64 FMA probe (pcg_fma_probe)",
-                     "traffic": None, "algorithmic_flops": eri_flops, "eri_pass_s": t_eri},
+        "roofline": {"bound": "tensor", "kernel": "k_ozt_gemm (tcgen05 Ozaki GEMM, the four MP2 quarter transforms)",
+                     "achieved": tc_flops / tc_t / 1e12, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                     "frac": (tc_flops / tc_t / 1e12) / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                     "traffic": None, "algorithmic_flops_per_launch": tc_flops / max(1, len(tl)),
+                     "launches": len(tl), "seconds": tc_t,
+                     "fp64_operand_and_output_bytes": tc_bytes},
+        "roofline_eri": {"bound": "fp64", "kernel": "ERI class kernels k_eri<*> (FP64 pipe)",
+                         "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                         "peak_source": "measured by bench.py FP64 FMA probe (pcg_fma_probe); MEASURED_PEAKS.json has no FP64 figure",
+                         "traffic": None, "algorithmic_flops": eri_flops, "eri_pass_s": t_eri},
         "peaks": {"fp64_tflops_probe": fp64_peak, "fp32_tflops_probe": fp32_peak,
                   "hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")},
         "fock_digest": {"s_per_build": t_fock, "store_bytes": store_bytes,

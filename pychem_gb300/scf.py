@@ -331,7 +331,7 @@ def _pair_rows(n, dev):
     return a * n + b
 
 
-def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None):
+def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None, timings=None):
     """(ia|jb) from the AO integrals by four quarter transforms, i, a with Co, Cv and
     j, b with Co2, Cv2 (default: the same; different for the opposite-spin block of
     UMP2).  eri: the dense tensor (n, n, n, n) or the bra-pair-packed one
@@ -345,7 +345,8 @@ def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None):
         T2 unpacked to [a'][i][a][b]                   T3[j][a' i a] = sum_b T2 Co2[b][j]
         T4[b'][j a' i] = sum_a T3 Cv2[a][b']           T4[b'][j][a'][i] = (i a'|j b').
     gemm="fp64": the same contraction by FP64 matrix products on the dense tensor
-    (cuBLAS DGEMM through torch), the cross-check."""
+    (cuBLAS DGEMM through torch), the cross-check.  timings (a list) receives
+    (M, N, K, (start, end) CUDA events) of every tensor-core launch."""
     n, o = Co.shape
     v = Cv.shape[1]
     Co2 = Co if Co2 is None else Co2
@@ -373,7 +374,13 @@ def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None):
 
     def quarter(X, rows, C, ncol):
         out = torch.empty(ncol * rows, dtype=torch.float64, device=dev)
+        if timings is not None:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record()
         ozaki_gemm_tc(X, C, out, rows, ncol, n, n, (ncol, 1), (1, rows), nslice=nslice)
+        if timings is not None:
+            ev[1].record()
+            timings.append((rows, ncol, n, ev))
         return out
 
     T1 = quarter(E, npair * n, Co, o)
