@@ -135,31 +135,109 @@ def cpu_eri_rate(atoms, basis, workers, target_s=10.0, seed=SEED):
     return rate, total, desc
 
 
+def cpu_full_estimate(atoms, basis, nocc, scf_iterations, threads, seed=SEED, target_s=3.0):
+    """CPU time of the whole RHF + MP2 workload through the oracle port (the pinned
+    restatement of the reference's integral, SCF and MP2 algorithms), on `threads`
+    host threads, from bounded samples:
+      ERIs: random windows of 512 consecutive screened quartets (threaded C blocks),
+        scaled to every quartet;
+      SCF: one Coulomb/exchange build over the sample's blocks, scaled to every
+        quartet and to the oracle SCF's iteration count (tests/golden/configs.json);
+      MP2: the first quarter transform (threaded C) over the sample for o_s
+        occupied orbitals, scaled to every quartet and all nocc; the other three
+        transforms (NumPy/BLAS) for one occupied orbital, times nocc.
+    Returns (seconds, description, breakdown)."""
+    import numpy as np
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    key = ("full", basis, tuple(tuple(a[2:]) for a in atoms))
+    b = O.Basis(atoms, basis)
+    if key not in _PLAN:
+        _PLAN[key] = b.quartet_array()
+    allq = _PLAN[key]
+    total = len(allq)
+    n = b.nbf
+    win = 512
+
+    def sample(m):
+        # whole windows of the canonical quartet order, so that the sample keeps the
+        # full run's locality (consecutive quartets share their bra pair)
+        k = max(1, m // win)
+        starts = rng.choice(max(1, total // win), size=min(k, max(1, total // win)), replace=False) * win
+        return np.concatenate([allq[s0:s0 + win] for s0 in np.sort(starts)])
+
+    probe = O.PackedStore(b, nthreads=threads, quads=sample(4096))
+    t0 = time.perf_counter()
+    O.PackedStore(b, nthreads=threads, quads=sample(4096))
+    per = (time.perf_counter() - t0) / 4096
+    quads = sample(int(min(total, max(4096, target_s / per))))
+    nq = len(quads)
+    t0 = time.perf_counter()
+    st = O.PackedStore(b, nthreads=threads, quads=quads)
+    t_eri = time.perf_counter() - t0
+    M = rng.normal(size=(n, n))
+    D = 0.01 * (M + M.T)
+    t0 = time.perf_counter()
+    st.jk(2.0 * D, D)
+    t_jk = time.perf_counter() - t0
+    o_s = max(1, min(nocc, threads))
+    C = rng.normal(size=(n, nocc + 1))
+    t0 = time.perf_counter()
+    T1 = st.mp2_first_quarter(C[:, :o_s])
+    t_q1 = time.perf_counter() - t0
+    del probe
+    # the other three transforms of one occupied orbital at full size (oracle.rmp2_packed)
+    v = n - nocc
+    Cv = rng.normal(size=(n, v))
+    Co = rng.normal(size=(n, nocc))
+    r_, s_ = np.tril_indices(n)
+    T1i = rng.normal(size=(n, n * (n + 1) // 2))
+    t0 = time.perf_counter()
+    T2 = Cv.T @ T1i
+    Mx = np.zeros((v, n, n))
+    Mx[:, r_, s_] = T2
+    Mx[:, s_, r_] = T2
+    np.einsum("alk,lj,kb->ajb", Mx, Co, Cv, optimize=True)
+    t_rest = time.perf_counter() - t0
+    del T1, T1i, Mx
+    scale = total / nq
+    parts = {"eri_s": t_eri * scale, "scf_s": scf_iterations * t_jk * scale,
+             "mp2_first_quarter_s": (nocc / o_s) * t_q1 * scale, "mp2_rest_s": nocc * t_rest}
+    desc = ("oracle port on %d thread(s): %d of %d screened shell quartets (random windows of 512 consecutive quartets) for the ERI, Coulomb/exchange "
+            "and first-MP2-transform kernels, scaled to every quartet, %d SCF iterations (the oracle SCF's own count) and "
+            "%d occupied orbitals; the other MP2 transforms timed for one occupied orbital x %d; extrapolated"
+            % (threads, nq, total, scf_iterations, nocc, nocc))
+    return sum(parts.values()), desc, parts
+
+
+def _c2_atoms_bohr():
+    from pychem_gb300 import workloads as W
+    return [(a[0], a[1], a[2] * 1.8897161646320724, a[3] * 1.8897161646320724, a[4] * 1.8897161646320724)
+            for a in W.water_cluster(seed=SEED)]
+
+
 def reference_arm(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    from pychem_gb300 import workloads as W
-    atoms_ang = W.water_cluster(seed=SEED)
-    atoms = [(a[0], a[1], a[2] * 1.8897161646320724, a[3] * 1.8897161646320724, a[4] * 1.8897161646320724)
-             for a in atoms_ang]
     from oracle import oracle as O
     O.build()
+    atoms = _c2_atoms_bohr()
+    ref = oracle_energies().get("c2_water16_631g", {})
+    iters = int(ref.get("scf_iterations", 31))
     cores = os.cpu_count() or 1
-    vals = []
-    desc = ""
+    vals, desc, parts = [], "", {}
     for k in range(args.warmup + args.steps):
-        rate, total, desc = cpu_eri_rate(atoms, "6-31G", cores, target_s=4.0, seed=SEED + k)
+        v, desc, parts = cpu_full_estimate(atoms, "6-31G", 80, iters, cores, seed=SEED + k, target_s=1.0)
         if k >= args.warmup:
-            vals.append(total / rate)
+            vals.append(v)
     v = statistics.mean(vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "basis": "6-31G", "seed": SEED},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
-                             "sample": desc + "; value = ERI phase extrapolated to every screened quartet "
-                                              "(a lower bound on the CPU time-to-convergence: SCF and MP2 not added)"},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": desc,
+                             "breakdown_s": parts},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -650,10 +728,11 @@ def gpu_arm(args):
     cpu = None
     if world == 1:
         atoms_b = [(a[0], a[1], *a[2]) for a in mol.atoms]
-        rate, total, desc = cpu_eri_rate(atoms_b, "6-31G", 1, target_s=12.0)
-        cpu = {"value": total / rate, "unit": "s", "cores": 1, "kind": "port",
-               "sample": desc + "; value = ERI phase extrapolated to every screened quartet (SCF and MP2 not added)",
-               "eri_quartets_per_s": rate}
+        ref_c2 = oracle_energies().get("c2_water16_631g", {})
+        cores = os.cpu_count() or 1
+        v_cpu, desc, parts = cpu_full_estimate(atoms_b, "6-31G", o, int(ref_c2.get("scf_iterations", 31)), cores,
+                                               target_s=3.0)
+        cpu = {"value": v_cpu, "unit": "s", "cores": cores, "kind": "port", "sample": desc, "breakdown_s": parts}
 
     achieved = eri_flops / t_eri / 1e12
     ref = oracle_energies().get("c2_water16_631g", {})

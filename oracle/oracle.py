@@ -252,10 +252,12 @@ class PackedStore:
     C oracle on several threads, for molecules whose dense N^4 tensor does not fit in
     host memory.  jk() and mp2_first_quarter() contract it without expanding it."""
 
-    def __init__(self, basis, nthreads=None, Q=None):
+    def __init__(self, basis, nthreads=None, Q=None, quads=None):
+        """quads: an explicit (nq, 4) quartet list instead of the screened one (a
+        sample, for timing)."""
         self.basis = basis
         self.nthreads = nthreads or os.cpu_count() or 1
-        self.quads = basis.quartet_array(Q)
+        self.quads = basis.quartet_array(Q) if quads is None else np.ascontiguousarray(quads, dtype=np.int32)
         ls = np.array([s[0] for s in basis.shells])
         dims = 2 * ls + 1
         size = dims[self.quads[:, 0]] * dims[self.quads[:, 1]] * dims[self.quads[:, 2]] * dims[self.quads[:, 3]]
