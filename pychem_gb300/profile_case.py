@@ -4,13 +4,15 @@
 
 cases:  water16 ((H2O)16 / 6-31G, 208 AO), water8 ((H2O)8, 104 AO), water4 ((H2O)4),
         alkane12 (C12H26 / cc-pVDZ, 298 AO), ensemble (256 perturbed small molecules,
-        6-31G, batched), mlp (the learned-guess network on 65,536 pairs)
+        6-31G, batched), mlp (the learned-guess network on 65,536 pairs), gemm (one
+        tensor-core Ozaki GEMM of the first MP2 transform's shape: 77,824 rows of 208
+        FP64 values (130 MB, more than L2) times 208 x 80)
 phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2);
         scattering (one j0(S r12) grid value at --S: Schwarz pass, quartet plan,
         integral store, contraction with the RHF densities, each timed);
         noci (the CI matrix of C2 / cc-pVDZ spin-flip doubles with CISD, 27
         determinants; --case is ignored);
-        for mlp: train (forward, loss, backward, Adam)
+        for mlp: train (forward, loss, backward, Adam); for gemm: tc
 """
 import argparse
 import time
@@ -30,10 +32,32 @@ CASES = {
 }
 
 
+def gemm_case(args):
+    """One pcg_ozaki_gemm_tc of the first MP2 quarter transform's shape per repeat."""
+    from .scf import ozaki_gemm_tc, ozaki_tc_status
+    M, N, K = 128 * 152 * 4, 80, 208
+    g = torch.Generator(device="cuda").manual_seed(1)
+    X = torch.randn(M, K, dtype=torch.float64, device="cuda", generator=g)
+    Y = torch.randn(K, N, dtype=torch.float64, device="cuda", generator=g)
+    C = torch.empty(N * M, dtype=torch.float64, device="cuda")
+    ozaki_gemm_tc(X, Y, C, M, N, K, K, (N, 1), (1, M))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.repeat):
+        ozaki_gemm_tc(X, Y, C, M, N, K, K, (N, 1), (1, M))
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.repeat
+    flops = 21 * 2.0 * M * N * K
+    print("tc gemm %d x %d x %d: %.3f ms per launch, %.1f TFLOP/s of digit-slice products, error flag %d"
+          % (M, N, K, ms, flops / ms / 1e9, ozaki_tc_status("cuda")))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="water16", choices=sorted(CASES) + ["ensemble", "mlp"])
-    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train", "scattering", "noci"])
+    ap.add_argument("--case", default="water16", choices=sorted(CASES) + ["ensemble", "mlp", "gemm"])
+    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train", "scattering", "noci", "tc"])
     ap.add_argument("--S", type=float, default=2.0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--repeat", type=int, default=1)
@@ -42,6 +66,8 @@ def main():
         return ensemble_case(args)
     if args.case == "mlp":
         return mlp_case(args)
+    if args.case == "gemm":
+        return gemm_case(args)
     if args.phase == "noci":
         return noci_case(args)
     mol = CASES[args.case]()
