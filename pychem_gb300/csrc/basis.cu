@@ -184,10 +184,38 @@ __device__ __forceinline__ double d_sph(int l, int r, int c) {
   }
 }
 
+// One warp per shell pair: lanes stride over the primitive pairs for S and T and over
+// (primitive pair, nucleus) items for the nuclear attraction V (the loop that
+// dominates: nuclei x primitive pairs), the Cartesian blocks are summed across the
+// warp with shuffles, and lane 0 applies the spherical transform and stores both
+// triangles of S and H (Methods/integrals.py:220-370).
+struct OePrim {
+  double U, z, oo2z, cc, P[3], PA[3], PB[3];
+};
+
+__device__ __forceinline__ OePrim oe_prim(const DevBasis& b, int A, int B, int ia, int ib, double r2) {
+  OePrim q;
+  const double* Ax = b.sh_xyz + 3 * A;
+  const double* Bx = b.sh_xyz + 3 * B;
+  const double al = b.pr_exp[b.sh_prim[A] + ia], be = b.pr_exp[b.sh_prim[B] + ib];
+  q.cc = b.pr_cc[b.sh_prim[A] + ia] * b.pr_cc[b.sh_prim[B] + ib];
+  q.z = al + be;
+  const double s = 1.0 / q.z;
+  q.oo2z = 0.5 * s;
+  q.U = pow(M_PI * s, 1.5) * exp(-al * be * s * r2);
+  for (int i = 0; i < 3; ++i) {
+    q.P[i] = (al * Ax[i] + be * Bx[i]) * s;
+    q.PA[i] = q.P[i] - Ax[i];
+    q.PB[i] = q.P[i] - Bx[i];
+  }
+  return q;
+}
+
 __global__ void k_one_electron(DevBasis b, BoysTable bt, int npair, const int* pA, const int* pB,
                                double* S, double* H) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= npair) return;
+  const int p = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (p >= npair) return;  // whole warps leave together
   const int A = pA[p], B = pB[p];
   const int la = b.sh_l[A], lb = b.sh_l[B];
   const int nca = d_ncart(la), ncb = d_ncart(lb);
@@ -197,18 +225,13 @@ __global__ void k_one_electron(DevBasis b, BoysTable bt, int npair, const int* p
   const double* Bx = b.sh_xyz + 3 * B;
   double r2 = 0.0;
   for (int i = 0; i < 3; ++i) r2 += (Ax[i] - Bx[i]) * (Ax[i] - Bx[i]);
-  for (int ia = 0; ia < b.sh_nprim[A]; ++ia)
-    for (int ib = 0; ib < b.sh_nprim[B]; ++ib) {
-      const double al = b.pr_exp[b.sh_prim[A] + ia], be = b.pr_exp[b.sh_prim[B] + ib];
-      const double cc = b.pr_cc[b.sh_prim[A] + ia] * b.pr_cc[b.sh_prim[B] + ib];
-      const double z = al + be, s = 1.0 / z, oo2z = 0.5 * s;
-      const double U = pow(M_PI * s, 1.5) * exp(-al * be * s * r2);
-      double P[3], PA[3], PB[3];
-      for (int i = 0; i < 3; ++i) {
-        P[i] = (al * Ax[i] + be * Bx[i]) * s;
-        PA[i] = P[i] - Ax[i];
-        PB[i] = P[i] - Bx[i];
-      }
+  const int npa = b.sh_nprim[A], npb = b.sh_nprim[B];
+  for (int item = lane; item < npa * npb; item += 32) {
+    const int ia = item / npb, ib = item % npb;
+    const double be = b.pr_exp[b.sh_prim[B] + ib];
+    const OePrim q = oe_prim(b, A, B, ia, ib, r2);
+    const double U = q.U, oo2z = q.oo2z, cc = q.cc;
+    const double *PA = q.PA, *PB = q.PB;
       // 1D overlap factors E[dir][i][j], i <= la, j <= lb + 2 (Obara-Saika)
       double E[3][3][5];
       for (int d = 0; d < 3; ++d) {
@@ -248,11 +271,18 @@ __global__ void k_one_electron(DevBasis b, BoysTable bt, int npair, const int* p
           Tc[ka * ncb + kb] += cc * U * t;
         }
       }
-      // nuclear attraction: Obara-Saika with auxiliary index over the molecule's nuclei
-      const int L = la + lb;
-      const int c0 = b.sh_at0 ? b.sh_at0[A] : 0;
-      const int c1 = b.sh_at0 ? c0 + b.sh_nat[A] : b.natom;
-      for (int c = c0; c < c1; ++c) {
+  }
+  // nuclear attraction: Obara-Saika with auxiliary index over the molecule's nuclei
+  const int L = la + lb;
+  const int c0 = b.sh_at0 ? b.sh_at0[A] : 0;
+  const int c1 = b.sh_at0 ? c0 + b.sh_nat[A] : b.natom;
+  const int nnuc = c1 - c0;
+  for (int item = lane; item < npa * npb * nnuc; item += 32) {
+    const int c = c0 + item % nnuc, pp = item / nnuc;
+    const OePrim q = oe_prim(b, A, B, pp / npb, pp % npb, r2);
+    const double U = q.U, oo2z = q.oo2z, cc = q.cc, z = q.z;
+    const double *P = q.P, *PA = q.PA, *PB = q.PB;
+    {
         const double* C = b.at_xyz + 3 * c;
         double PC[3], pc2 = 0.0;
         for (int i = 0; i < 3; ++i) { PC[i] = P[i] - C[i]; pc2 += PC[i] * PC[i]; }
@@ -306,6 +336,18 @@ __global__ void k_one_electron(DevBasis b, BoysTable bt, int npair, const int* p
           }
       }
     }
+  // sum the lanes' Cartesian blocks
+  for (int i = 0; i < nca * ncb; ++i) {
+    double sv = Sc[i], tv = Tc[i], vv = Vc[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sv += __shfl_xor_sync(0xffffffffu, sv, o);
+      tv += __shfl_xor_sync(0xffffffffu, tv, o);
+      vv += __shfl_xor_sync(0xffffffffu, vv, o);
+    }
+    Sc[i] = sv; Tc[i] = tv; Vc[i] = vv;
+  }
+  if (lane != 0) return;
   // spherical transform and store both triangles
   const int nsa = 2 * la + 1, nsb = 2 * lb + 1;
   const int oa = b.sh_ao[A], ob = b.sh_ao[B];
@@ -336,7 +378,7 @@ __global__ void k_one_electron(DevBasis b, BoysTable bt, int npair, const int* p
 int pcg_launch_one_electron(const DevBasis& b, const BoysTable& bt, int npair, const int* pA, const int* pB,
                             double* S, double* H, cudaStream_t s) {
   if (npair <= 0) return PCG_OK;
-  k_one_electron<<<(npair + 63) / 64, 64, 0, s>>>(b, bt, npair, pA, pB, S, H);
+  k_one_electron<<<(unsigned)(((long long)npair * 32 + 127) / 128), 128, 0, s>>>(b, bt, npair, pA, pB, S, H);
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;
 }

@@ -49,14 +49,15 @@ def atomic_density(symbol, Z, basis, device="cuda", iters=40, damping=0.5, max_l
     S, H = eng.S, eng.H
     s, U = eigen.eigh(S)
     keep = s > 1e-6
-    X = U[:, keep] * s[keep].rsqrt()
-    Xt = X.T.contiguous()
+    X = (U[:, keep] * s[keep].rsqrt()).contiguous()
+
+    from .dense import mm
 
     def density(F):
-        e, Cp = eigen.eigh(Xt @ F @ X)
-        C = X @ Cp
+        e, Cp = eigen.eigh(mm(X, mm(F, X), ta=True))
+        C = mm(X, Cp)
         f = _fractional_occupations(e, ne / 2.0)
-        return (C * f) @ C.T
+        return mm(C * f, C, tb=True)
 
     D = density(H)
     for _ in range(iters):
