@@ -11,7 +11,9 @@ phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2);
         scattering (one j0(S r12) grid value at --S: Schwarz pass, quartet plan,
         integral store, contraction with the RHF densities, each timed);
         noci (the CI matrix of C2 / cc-pVDZ spin-flip doubles with CISD, 27
-        determinants; --case is ignored);
+        determinants; --case is ignored); codensity (J/K of 756 random non-symmetric
+        co-densities of C2 / cc-pVDZ in one pcg_digest_class_co pass per class, the
+        NOCI digestion without the host's SVDs; --case is ignored);
         for mlp: train (forward, loss, backward, Adam); for gemm: tc
 """
 import argparse
@@ -30,6 +32,22 @@ CASES = {
     "water4": lambda: Molecule(W.water_cluster(nx=2, ny=2, nz=1), "6-31G"),
     "alkane12": lambda: Molecule(W.alkane(12), "cc-pVDZ"),
 }
+
+
+def codensity_case(args):
+    """J/K of 756 random non-symmetric co-densities of C2 / cc-pVDZ (28 AO), one
+    GpuEngine.coulomb_exchange call per repeat."""
+    mol = Molecule([["C", 6.0, 0.0, 0.0, 0.0], ["C", 6.0, 1.25, 0.0, 0.0]], "cc-pVDZ")
+    eng = GpuEngine(mol).prepare()
+    g = torch.Generator(device="cuda").manual_seed(4)
+    W = torch.randn(756, eng.nbf, eng.nbf, dtype=torch.float64, device="cuda", generator=g) * 0.05
+    eng.coulomb_exchange(W)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.repeat):
+        eng.coulomb_exchange(W)
+    torch.cuda.synchronize()
+    print("codensity C2 cc-pVDZ: 756 co-densities, %.3f ms per J/K pass" % ((time.perf_counter() - t0) * 1e3 / args.repeat))
 
 
 def gemm_case(args):
@@ -57,7 +75,7 @@ def gemm_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="water16", choices=sorted(CASES) + ["ensemble", "mlp", "gemm"])
-    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train", "scattering", "noci", "tc"])
+    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train", "scattering", "noci", "tc", "codensity"])
     ap.add_argument("--S", type=float, default=2.0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--repeat", type=int, default=1)
@@ -70,6 +88,8 @@ def main():
         return gemm_case(args)
     if args.phase == "noci":
         return noci_case(args)
+    if args.phase == "codensity":
+        return codensity_case(args)
     mol = CASES[args.case]()
     if args.phase == "scattering":
         return scattering_case(args, mol)
