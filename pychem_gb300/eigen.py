@@ -147,6 +147,9 @@ def refine_projector(A, X, nocc, steps=2, check=False):
         R, S = _rs(A, X)
         E = dense.oa_correction(S, R, nocc, 0, lam=lam)
         X = _step(X, E)
+    # the occupied-virtual rotations of large steps leave O(E^2) non-orthogonality;
+    # one Newton-Schulz step X <- X + X (I - X^T X)/2 removes it quadratically
+    X = orthonormalize(X, steps=1)
     if not check:
         return lam, X
     R, S = _rs(A, X)
@@ -155,26 +158,32 @@ def refine_projector(A, X, nocc, steps=2, check=False):
     return lam, X, chk
 
 
-def _split_point(w, n):
-    """Where to slice an ascending spectrum of size n > 136: the largest gap among the
-    positions that leave both parts at most 136 long (the middle third when none do)."""
-    lo, hi = max(1, n - FP64_JACOBI_MAX_N), min(n - 1, FP64_JACOBI_MAX_N)
-    if lo > hi:
-        lo, hi = n // 3, (2 * n) // 3
+EXACT_BLOCK = 64    # exact_eigh finishes blocks up to this size with the FP64 Jacobi kernel
+
+
+def _split_point(w, n, base=EXACT_BLOCK):
+    """Where to slice an ascending spectrum of size n > base: the largest gap among the
+    positions that leave both parts at most base long, or, when that window is
+    narrower than a quarter of n, among the middle half."""
+    lo, hi = max(1, n - base), min(n - 1, base)
+    if hi - lo < n // 4:
+        lo, hi = n // 4, (3 * n) // 4
     gaps = w[lo:hi + 1] - w[lo - 1:hi]
     return lo + int(torch.argmax(gaps))
 
 
 def exact_eigh(A, X_prev=None, steps=4):
     """Eigenpairs of one symmetric A to FP64 accuracy on the library's kernels, by
-    spectrum slicing: n <= 136, the FP64 Jacobi kernel started from the FP32 Jacobi
-    vectors (so it needs few sweeps); larger n, the FP32 Jacobi vectors (from X_prev
-    when given), a split at the largest gap that keeps both parts small, projector
+    spectrum slicing: n <= 64, the FP64 Jacobi kernel (one CTA: its cost grows as n^3
+    on the thin FP64 pipe) started from the FP32 Jacobi vectors (so it needs few
+    sweeps); larger n, the FP32 Jacobi vectors (from X_prev
+    when given), a split at the largest gap that keeps both parts at most 64 (or in
+    the middle half), projector
     refinement that decouples the two invariant subspaces in FP64, and the same on
     each part's projected matrix.  Near-degenerate clusters end up inside one part,
     where Jacobi resolves them."""
     n = A.shape[-1]
-    if n <= FP64_JACOBI_MAX_N:
+    if n <= EXACT_BLOCK:
         _, V32 = eigh32_own(A, X_prev)
         V = orthonormalize(V32)
         Ap = dense.mm(V, dense.mm(A, V), ta=True)
