@@ -685,7 +685,7 @@ def gpu_arm(args):
     # flops of the digit-slice products, 2 M N Kp per product, 21 products (6 slices,
     # levels up to 7), Kp = K rounded up to the 32-column chunk
     from pychem_gb300.scf import mp2_transform, ozaki_tc_status
-    Ep = eng.dense_eri_pairs()
+    Ep = eng.dense_eri_pairs(compact=True)
     tc_t, tc_flops = 0.0, 0.0
     tc_runs = []
     for _ in range(3):

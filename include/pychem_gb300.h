@@ -250,14 +250,23 @@ int pcg_fock_build_noalloc(const pcg_basis_t *basis, const pcg_pairs_t *pairs, i
 int pcg_dense_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
                     int ntask, const double *store, double *eri, void *stream);
 
-/* The same with the bra pair packed, E[pair(a, b)][c][d] with a >= b and pair(a, b) =
- * a(a+1)/2 + b (nbf(nbf+1)/2 x nbf x nbf doubles): the input of the first MP2
- * quarter transform, which keeps the bra symmetry (Methods/mp2.py:43-69 transforms
- * the full tensor). */
+/* The same with the bra pair packed, E[row(a, b)][c][d] with a >= b: the input of the
+ * first MP2 quarter transform, which keeps the bra symmetry (Methods/mp2.py:43-69
+ * transforms the full tensor).  row(a, b) = pairmap[pair(a, b)], pair(a, b) =
+ * a(a+1)/2 + b, so that only the AO pairs some stored quartet contains get rows
+ * (pairmap NULL: row = pair(a, b), nbf(nbf+1)/2 rows); E: rows x nbf x nbf doubles. */
 int pcg_dense_pairs_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks,
-                          int ntask, const double *store, double *E, void *stream);
-/* out[r][a][b] = in[r][pair(a, b)] for r < R, a, b < n (pair-packed rows unpacked). */
-int pcg_unpack_pairs(long long R, int n, const double *in, double *out, void *stream);
+                          int ntask, const double *store, const int *pairmap, double *E, void *stream);
+/* The symmetric pair matrix of the compact rows: M[pairmap[pair(a, b)]][pairmap[pair(c, d)]]
+ * = (ab|cd) (both triangles; rows x rows doubles, zeroed by the caller), for the
+ * elements whose bra and ket pairs both have rows; with pcg_unpack_pairs(rows, nbf, rows,
+ * pairmap, M, E) it gives the tensor of pcg_dense_pairs_class with half the scattered
+ * stores. */
+int pcg_sym_pairs_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks, int ntask,
+                        const double *store, const int *pairmap, long long rows, double *M, void *stream);
+/* out[r][a][b] = in[r * len + pairmap[pair(a, b)]] (0 where pairmap is -1) for r < R,
+ * a, b < n: pair-packed rows of length len unpacked (pairmap NULL: the pair itself). */
+int pcg_unpack_pairs(long long R, int n, int len, const int *pairmap, const double *in, double *out, void *stream);
 
 /* FP64-accurate GEMM with every Ozaki level in one tcgen05 tensor-core kernel (no
  * upstream counterpart; it carries the AO->MO transform of Methods/mp2.py:43-69 and
@@ -297,6 +306,14 @@ int pcg_oa_correction(int n, int nocc, int mode, const double *delta, const doub
                       double *lam, void *stream);
 int pcg_diis_step(long long len, int cap, int *state, const double *F, const double *R, double *focks,
                   double *resids, double *Bm, double *row, double *coef, double *Fx, void *stream);
+
+/* Closed-shell MP2 energy sums (replaces the numpy sums of Methods/mp2.py:71-94): from
+ * X(i,a,j,b) = (ia|jb) stored at ((b*o + j)*v + a)*o + i and the orbital energies eo
+ * (o), ev (v), part[2p] and part[2p+1] (p = b*o + j, o*v blocks) receive block partials
+ * of s1 = sum X^2/D and s2 = sum X(i,a,j,b) X(i,b,j,a)/D, D = e_i + e_j - e_a - e_b.
+ * E_MP2 = 2 s1 - s2; same spin s1 - s2, opposite spin s1.  One kernel. */
+int pcg_mp2_pair_sums(int o, int v, const double *X, const double *eo, const double *ev, double *part,
+                      void *stream);
 
 /* Batched symmetric eigensolver (no upstream counterpart; replaces the LAPACK eigh of
  * Methods/hartree_fock.py:172-175,226): parallel cyclic Jacobi, one CTA per matrix.

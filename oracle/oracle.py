@@ -585,10 +585,11 @@ def uhf(S, H, eri, na, nb, e_nuc, cuhf=False, max_iter=300, e_tol=1e-11, d_tol=1
     return dict(E=E, Ca=Ca, Cb=Cb, ea=ea, eb=eb, Da=Da, Db=Db, Fa=Fa, Fb=Fb, iterations=it, converged=converged)
 
 
-def ump2(Ca, Cb, ea, eb, eri, na, nb):
+def ump2(Ca, Cb, ea, eb, eri, na, nb, scale=None):
     """Unrestricted MP2 correlation energy, Methods/mp2.py:43-101: same-spin
     sum over i >= j, p >= q of (<ip|jq> - <iq|jp>)^2 / D, opposite-spin sum of
-    <ip|jq>^2 / D, with the orbital energies of the final Fock matrices."""
+    <ip|jq>^2 / D, with the orbital energies of the final Fock matrices; scale =
+    (c_ss, c_os) weights the two parts (SCS / SOS, Methods/mp2.py:97-107)."""
     def mo(C1, C2, o1, o2):
         return np.einsum("pi,qa,rj,sb,pqrs->iajb", C1[:, :o1], C1[:, o1:], C2[:, :o2], C2[:, o2:], eri, optimize=True)
 
@@ -602,7 +603,10 @@ def ump2(Ca, Cb, ea, eb, eri, na, nb):
     g = mo(Ca, Cb, na, nb)
     den = (ea[:na, None, None, None] - ea[None, na:, None, None] + eb[None, None, :nb, None]
            - eb[None, None, None, nb:])
-    return same(Ca, ea, na) + same(Cb, eb, nb) + float(np.sum(g * g / den))
+    e_ss, e_os = same(Ca, ea, na) + same(Cb, eb, nb), float(np.sum(g * g / den))
+    if scale is not None:
+        return scale[0] * e_ss + scale[1] * e_os
+    return e_ss + e_os
 
 
 # ------------------------------------------------------------------------------------

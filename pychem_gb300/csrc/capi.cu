@@ -171,19 +171,33 @@ int pcg_dense_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs,
 }
 
 int pcg_dense_pairs_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
-                          const double* store, double* E, void* stream) {
+                          const double* store, const int* pairmap, double* E, void* stream) {
   if (cls < 0 || cls > 20 || !basis || !pairs || !E) {
     pcg_set_error("pcg_dense_pairs_class: bad arguments");
     return PCG_ERR_ARG;
   }
   if (basis->sh_blk) { pcg_set_error("pcg_dense_pairs_class: one molecule only"); return PCG_ERR_UNSUPPORTED; }
-  return pcg_launch_dense_pairs(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, E,
+  return pcg_launch_dense_pairs(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, pairmap, E,
                                 (cudaStream_t)stream);
 }
 
-int pcg_unpack_pairs(long long R, int n, const double* in, double* out, void* stream) {
-  if (R < 0 || n < 1 || !in || !out) { pcg_set_error("pcg_unpack_pairs: bad arguments"); return PCG_ERR_ARG; }
-  return pcg_launch_unpack_pairs(R, n, in, out, (cudaStream_t)stream);
+int pcg_sym_pairs_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pairs, const int* tasks, int ntask,
+                        const double* store, const int* pairmap, long long rows, double* M, void* stream) {
+  if (cls < 0 || cls > 20 || !basis || !pairs || !pairmap || rows < 1 || !M || (ntask > 0 && (!tasks || !store))) {
+    pcg_set_error("pcg_sym_pairs_class: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  if (basis->sh_blk) { pcg_set_error("pcg_sym_pairs_class: one molecule only"); return PCG_ERR_UNSUPPORTED; }
+  return pcg_launch_sym_pairs(cls, to_dev(basis), to_dev(pairs), (const int2*)tasks, ntask, store, pairmap, rows, M,
+                              (cudaStream_t)stream);
+}
+
+int pcg_unpack_pairs(long long R, int n, int len, const int* pairmap, const double* in, double* out, void* stream) {
+  if (R < 0 || n < 1 || len < 1 || !in || !out || (!pairmap && len < n * (n + 1) / 2)) {
+    pcg_set_error("pcg_unpack_pairs: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  return pcg_launch_unpack_pairs(R, n, len, pairmap, in, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

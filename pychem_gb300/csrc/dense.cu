@@ -225,3 +225,68 @@ extern "C" int pcg_diis_step(long long len, int cap, int* state, const double* F
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;
 }
+
+// ------------------------------------------------------------------------------------
+// Closed-shell MP2 energy sums over the transformed integrals X(i,a,j,b) = (ia|jb)
+// (Methods/mp2.py:71-94), X stored b-major: X(i,a,j,b) at ((b*o + j)*v + a)*o + i, so
+// that both X(i,a,j,b) and its exchange partner X(i,b,j,a) are read along i.
+//   s1 = sum X(i,a,j,b)^2 / D,  s2 = sum X(i,a,j,b) X(i,b,j,a) / D,
+//   D = e_i + e_j - e_a - e_b.
+// Both summands are symmetric under (i,a) <-> (j,b); block p = b*o + j takes the
+// pairs q = a*o + i <= p, weight 2 below the diagonal.  1/D: the FP32 reciprocal and
+// one Newton step in FP64 (relative error ~ 2^-46).  part[2p], part[2p+1]: the block's
+// s1 and s2 (summed on the host side of the call, in a fixed order).
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_mp2_pair_sums(int o, int v, const double* __restrict__ X,
+                                                       const double* __restrict__ eo, const double* __restrict__ ev,
+                                                       double* __restrict__ part) {
+  extern __shared__ double e_sh[];                 // eo (o), then ev (v)
+  for (int t = threadIdx.x; t < o + v; t += blockDim.x) e_sh[t] = t < o ? eo[t] : ev[t - o];
+  __syncthreads();
+  const int p = blockIdx.x, b = p / o, j = p % o;
+  const double ejb = e_sh[j] - e_sh[o + b];
+  const double* Xp = X + (size_t)p * v * o;                       // X(., ., j, b)
+  const int step = blockDim.x, da = step / o, di = step % o;
+  int a = threadIdx.x / o, i = threadIdx.x % o;
+  double s1 = 0.0, s2 = 0.0;
+  for (int q = threadIdx.x; q <= p; q += step) {
+    const double x = Xp[q];
+    const double xe = X[((size_t)(a * o + j) * v + b) * o + i];   // X(i, b, j, a)
+    const double d = (e_sh[i] - e_sh[o + a]) + ejb;
+    double r = (double)__frcp_rn((float)d);
+    r = fma(r, fma(-d, r, 1.0), r);
+    const double t = (q < p ? 2.0 : 1.0) * x * r;
+    s1 = fma(x, t, s1);
+    s2 = fma(xe, t, s2);
+    i += di; a += da;
+    if (i >= o) { i -= o; ++a; }
+  }
+  for (int off = 16; off; off >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, off);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, off);
+  }
+  __shared__ double red[2][8];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[0][w] = s1; red[1][w] = s2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r1 = 0.0, r2 = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { r1 += red[0][k]; r2 += red[1][k]; }
+    part[2 * (size_t)p] = r1;
+    part[2 * (size_t)p + 1] = r2;
+  }
+}
+
+extern "C" int pcg_mp2_pair_sums(int o, int v, const double* X, const double* eo, const double* ev, double* part,
+                                 void* stream) {
+  if (o < 1 || v < 1 || !X || !eo || !ev || !part || (long long)o * v > 0x7fffffffLL ||
+      (size_t)(o + v) * sizeof(double) > 200 * 1024) {
+    pcg_set_error("pcg_mp2_pair_sums: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  const size_t sh = (size_t)(o + v) * sizeof(double);
+  if (sh > 48 * 1024) PCG_CUDA(cudaFuncSetAttribute(k_mp2_pair_sums, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  k_mp2_pair_sums<<<o * v, 256, sh, (cudaStream_t)stream>>>(o, v, X, eo, ev, part);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}

@@ -152,7 +152,8 @@ __device__ __forceinline__ size_t ao_pair(size_t a, size_t b) { return a >= b ? 
 
 template <int NA, int NB, int NC, int ND>
 __global__ void k_dense_pairs(DevBasis b, DevPairsExt pr, const int2* __restrict__ tasks, int ntask,
-                              const double* __restrict__ store, double* __restrict__ E) {
+                              const double* __restrict__ store, const int* __restrict__ pmap,
+                              double* __restrict__ E) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntask) return;
   const int2 tk = tasks[t];
@@ -161,37 +162,78 @@ __global__ void k_dense_pairs(DevBasis b, DevPairsExt pr, const int2* __restrict
   const size_t n = b.nbf;
   for (int i = 0; i < NA; ++i)
     for (int j = 0; j < NB; ++j) {
-      const size_t pab = ao_pair(oa + i, ob + j);
+      const long long pab = pmap ? (long long)__ldg(pmap + ao_pair(oa + i, ob + j)) : (long long)ao_pair(oa + i, ob + j);
       for (int k = 0; k < NC; ++k)
         for (int l = 0; l < ND; ++l) {
           const double v = store[(size_t)(((i * NB + j) * NC + k) * ND + l) * ntask + t];
           const size_t a = oa + i, bb = ob + j, c = oc + k, d = od + l;
-          const size_t pcd = ao_pair(c, d);
-          E[(pab * n + c) * n + d] = v;
-          E[(pab * n + d) * n + c] = v;
-          E[(pcd * n + a) * n + bb] = v;
-          E[(pcd * n + bb) * n + a] = v;
+          const long long pcd = pmap ? (long long)__ldg(pmap + ao_pair(c, d)) : (long long)ao_pair(c, d);
+          // a pair without a row (map -1) is written nowhere
+          if (pab >= 0) {
+            E[((size_t)pab * n + c) * n + d] = v;
+            E[((size_t)pab * n + d) * n + c] = v;
+          }
+          if (pcd >= 0) {
+            E[((size_t)pcd * n + a) * n + bb] = v;
+            E[((size_t)pcd * n + bb) * n + a] = v;
+          }
         }
     }
 }
 
-// out[r][a][b] = in[r][pair(a, b)] for r < R, a, b < n
-__global__ void k_unpack_pairs(long long R, int n, const double* __restrict__ in, double* __restrict__ out) {
+// The symmetric pair matrix of the compact rows: M[map(pair(a, b))][map(pair(c, d))] =
+// (ab|cd) for the AO pairs with rows (rows x rows, both triangles written); an element
+// whose bra or ket pair has no row belongs to the diagonal quartet of such a pair and
+// is left out with it.  Two stores per stored element instead of four.
+template <int NA, int NB, int NC, int ND>
+__global__ void k_sym_pairs(DevBasis b, DevPairsExt pr, const int2* __restrict__ tasks, int ntask,
+                            const double* __restrict__ store, const int* __restrict__ pmap, long long rows,
+                            double* __restrict__ M) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  const int2 tk = tasks[t];
+  const int oa = b.sh_ao[pr.p.A[tk.x]], ob = b.sh_ao[pr.p.B[tk.x]];
+  const int oc = b.sh_ao[pr.p.A[tk.y]], od = b.sh_ao[pr.p.B[tk.y]];
+  int pcd[NC * ND];
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int l = 0; l < ND; ++l) pcd[k * ND + l] = __ldg(pmap + ao_pair(oc + k, od + l));
+  for (int i = 0; i < NA; ++i)
+    for (int j = 0; j < NB; ++j) {
+      const int pab = __ldg(pmap + ao_pair(oa + i, ob + j));
+      if (pab < 0) continue;
+#pragma unroll
+      for (int kl = 0; kl < NC * ND; ++kl) {
+        if (pcd[kl] < 0) continue;
+        const double v = store[(size_t)((i * NB + j) * NC * ND + kl) * ntask + t];
+        M[(size_t)pab * rows + pcd[kl]] = v;
+        M[(size_t)pcd[kl] * rows + pab] = v;
+      }
+    }
+}
+
+// out[r][a][b] = in[r][map(pair(a, b))] for r < R, a, b < n: rows of `in` have `len`
+// entries; pmap (optional) gives the row position of each pair or -1 for a pair that
+// is not stored (its value is 0); without pmap the position is pair(a, b) itself
+__global__ void k_unpack_pairs(long long R, int n, int len, const int* __restrict__ pmap,
+                               const double* __restrict__ in, double* __restrict__ out) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nn = (long long)n * n;
   if (idx >= R * nn) return;
   const long long r = idx / nn;
   const int ab = (int)(idx - r * nn), a = ab / n, bb = ab - a * n;
-  out[idx] = __ldg(in + r * (nn + n) / 2 + ao_pair(a, bb));
+  const long long q = pmap ? (long long)__ldg(pmap + ao_pair(a, bb)) : (long long)ao_pair(a, bb);
+  out[idx] = q >= 0 ? __ldg(in + r * len + q) : 0.0;
 }
 
 int pcg_launch_dense_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
-                           const double* store, double* E, cudaStream_t s) {
+                           const double* store, const int* pmap, double* E, cudaStream_t s) {
   if (ntask <= 0) return PCG_OK;
   const int threads = 128, blocks = (ntask + threads - 1) / threads;
   switch (cls) {
 #define X(id, a, bb, c, d) \
-  case id: k_dense_pairs<a, bb, c, d><<<blocks, threads, 0, s>>>(b, pr, tasks, ntask, store, E); break;
+  case id: k_dense_pairs<a, bb, c, d><<<blocks, threads, 0, s>>>(b, pr, tasks, ntask, store, pmap, E); break;
     PCG_SHAPE_CASES(X)
 #undef X
     default: pcg_set_error("pcg_dense_pairs_class: class id out of range"); return PCG_ERR_ARG;
@@ -200,10 +242,26 @@ int pcg_launch_dense_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, co
   return PCG_OK;
 }
 
-int pcg_launch_unpack_pairs(long long R, int n, const double* in, double* out, cudaStream_t s) {
+int pcg_launch_sym_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
+                         const double* store, const int* pmap, long long rows, double* M, cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  const int threads = 128, blocks = (ntask + threads - 1) / threads;
+  switch (cls) {
+#define X(id, a, bb, c, d) \
+  case id: k_sym_pairs<a, bb, c, d><<<blocks, threads, 0, s>>>(b, pr, tasks, ntask, store, pmap, rows, M); break;
+    PCG_SHAPE_CASES(X)
+#undef X
+    default: pcg_set_error("pcg_sym_pairs_class: class id out of range"); return PCG_ERR_ARG;
+  }
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+int pcg_launch_unpack_pairs(long long R, int n, int len, const int* pmap, const double* in, double* out,
+                            cudaStream_t s) {
   const long long total = R * n * n;
   if (total <= 0) return PCG_OK;
-  k_unpack_pairs<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(R, n, in, out);
+  k_unpack_pairs<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(R, n, len, pmap, in, out);
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;
 }

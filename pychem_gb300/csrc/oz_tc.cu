@@ -216,26 +216,12 @@ __global__ void __launch_bounds__(OZT_THREADS, 1)
 #pragma unroll 1
         for (int p = 0; p < NS; ++p) tma_load_2d(smem_u32(yt + p * Cfg::YT), &ymap, k0, p * Npad + n0, &bars[6 + st]);
       }
-      unsigned long long G[8];
-      int neg = 0;
+      unsigned w[4][NS];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        G[j] = oz_biased<NS>(v[j], emax);
-        neg |= (int)((unsigned long long)__double_as_longlong(v[j]) >> 63) << j;
-      }
+      for (int hh = 0; hh < 4; ++hh) oz_digits_bf16x2<NS>(v[2 * hh], v[2 * hh + 1], emax, w[hh]);
 #pragma unroll
-      for (int p = 1; p <= NS; ++p) {
-        uint32_t w[4];
-#pragma unroll
-        for (int hh = 0; hh < 4; ++hh) {
-          int d0 = oz_digit<NS>(G[2 * hh], p), d1 = oz_digit<NS>(G[2 * hh + 1], p);
-          d0 = ((neg >> (2 * hh)) & 1) ? -d0 : d0;
-          d1 = ((neg >> (2 * hh + 1)) & 1) ? -d1 : d1;
-          __nv_bfloat162 b2 = __floats2bfloat162_rn((float)d0, (float)d1);
-          w[hh] = *(uint32_t*)&b2;
-        }
-        *(uint4*)(xt + (p - 1) * Cfg::XT + off) = make_uint4(w[0], w[1], w[2], w[3]);
-      }
+      for (int p = 0; p < NS; ++p)
+        *(uint4*)(xt + p * Cfg::XT + off) = make_uint4(w[0][p], w[1][p], w[2][p], w[3][p]);
       fence_proxy_async_smem();
       mbar_arrive(&bars[st]);
     }

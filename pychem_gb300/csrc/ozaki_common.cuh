@@ -2,6 +2,7 @@
 // digit split of an FP64 value against its vector's exponent, and the exact rounding
 // of an int64 level sum times a power of two to FP64.  Integer operations only.
 #pragma once
+#include <cuda_bf16.h>
 #include <stdint.h>
 
 #ifndef OZ_BETA
@@ -77,3 +78,53 @@ __device__ __forceinline__ double oz_ll_scaled(long long acc, int e) {
   return __longlong_as_double((long long)((sign << 63) | ((unsigned long long)ef << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
+// The same digits for two values at once, packed as BF16 pairs: w[p-1] holds digit p of
+// x0 (low half) and x1 (high half).  32-bit work only: the top 7 NS + 1 bits of
+// |x| 2^{63-e} are one right shift of the 53-bit mantissa (the shift is at least
+// 52 - 7 NS >= 3 because |x| < 2^e), the bias of oz_biased (in these units: 64 at
+// every digit and 1 at the rounding bit) is a constant, a digit is one shift and mask,
+// u - 64 becomes an exact float as (2^23 + u) - (2^23 + 64), and the signs are applied
+// to the packed pair with one XOR.  Identical digits to oz_digits.
+template <int NS>
+__device__ __forceinline__ unsigned long long oz_top_biased(double x, int emax) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int ex = (int)((hi >> 20) & 0x7FFu);
+  const int e = emax ? emax - 1022 : 0;
+  const int sft = (62 - OZ_BETA * NS) - (ex - 1012 - e);
+  unsigned long long R = 0;
+  if (ex != 0 && emax != 0 && sft < 53) {
+    const unsigned mh = (hi & 0xFFFFFu) | 0x100000u;
+    unsigned rl, rh;
+    if (sft < 32) {
+      rl = __funnelshift_r(lo, mh, sft);
+      rh = mh >> sft;
+    } else {
+      rl = mh >> (sft - 32);
+      rh = 0u;
+    }
+    R = ((unsigned long long)rh << 32) | rl;
+  }
+  unsigned long long B = 1ull;
+#pragma unroll
+  for (int p = 1; p <= NS; ++p) B += 64ull << (1 + OZ_BETA * (NS - p));
+  return R + B;
+}
+
+__device__ __forceinline__ float oz_u7_to_float(unsigned u) {  // u - 64 for u in [0, 255], exact
+  return __int_as_float(0x4B000000 | (int)u) - 8388672.0f;
+}
+
+template <int NS>
+__device__ __forceinline__ void oz_digits_bf16x2(double x0, double x1, int emax, unsigned* w) {
+  const unsigned long long G0 = oz_top_biased<NS>(x0, emax), G1 = oz_top_biased<NS>(x1, emax);
+  const unsigned sg = ((unsigned)__double2hiint(x0) >> 31 ? 0x8000u : 0u) |
+                      ((unsigned)__double2hiint(x1) >> 31 ? 0x80000000u : 0u);
+#pragma unroll
+  for (int p = 1; p <= NS; ++p) {
+    const int b = 1 + OZ_BETA * (NS - p);
+    const unsigned u0 = p == 1 ? (unsigned)(G0 >> b) : (unsigned)(G0 >> b) & 127u;
+    const unsigned u1 = p == 1 ? (unsigned)(G1 >> b) : (unsigned)(G1 >> b) & 127u;
+    __nv_bfloat162 b2 = __floats2bfloat162_rn(oz_u7_to_float(u0), oz_u7_to_float(u1));
+    w[p - 1] = *(unsigned*)&b2 ^ sg;
+  }
+}

@@ -54,8 +54,11 @@ int pcg_launch_digest_u(int cls, const DevBasis& b, const DevPairsExt& pr, const
 int pcg_launch_digest_co(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                          const double* store, int nd, const double* W, double* GJ, double* GK, cudaStream_t s);
 int pcg_launch_dense_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
-                           const double* store, double* E, cudaStream_t s);
-int pcg_launch_unpack_pairs(long long R, int n, const double* in, double* out, cudaStream_t s);
+                           const double* store, const int* pmap, double* E, cudaStream_t s);
+int pcg_launch_sym_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
+                         const double* store, const int* pmap, long long rows, double* M, cudaStream_t s);
+int pcg_launch_unpack_pairs(long long R, int n, int len, const int* pmap, const double* in, double* out,
+                            cudaStream_t s);
 int pcg_launch_dense(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                      const double* store, double* eri, cudaStream_t s);
 

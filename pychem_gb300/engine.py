@@ -403,16 +403,70 @@ class GpuEngine:
                           _stream())
         return 0.25 * (GJ + GJ.transpose(1, 2)), -0.5 * GK
 
-    def dense_eri_pairs(self):
-        """The dense tensor with the bra pair packed: E[pair(a, b)][c][d], a >= b,
-        pair(a, b) = a(a+1)/2 + b (nbf(nbf+1)/2 x nbf x nbf), zero where screened out."""
+    def stored_pair_map(self):
+        """(map, count): for every AO pair a >= b, at pair(a, b) = a(a+1)/2 + b, its row
+        in a compact pair-packed tensor, or -1 when its shell pair is in no stored
+        quartet but its own diagonal one (ab|ab) -- the quartet upstream always
+        computes, whose value is below (1e-8 / max Q)^2 ~ 1e-16 when the pair fails
+        every Schwarz test, and which MP2 then leaves out; rows follow pair order.  On
+        a 16-water cluster 56 % of the AO pairs have rows."""
         n = self.nbf
-        E = torch.zeros(n * (n + 1) // 2 * n * n, dtype=torch.float64, device=self.dev)
+        nao2 = n * (n + 1) // 2
+        if getattr(self, "_pair_ao", None) is None or self._pair_ao[0] is not self.h_pairs:
+            # the AO pairs of every shell pair (up to 5 x 5), nao2 where a slot is empty
+            a, hp = self.h_basis, self.h_pairs
+            ao, dim = a["sh_ao"].astype(np.int64), 2 * a["sh_l"].astype(np.int64) + 1
+            i, j = np.divmod(np.arange(25), 5)
+            fa = ao[hp["A"]][:, None] + i[None, :]
+            fb = ao[hp["B"]][:, None] + j[None, :]
+            ok = (i[None, :] < dim[hp["A"]][:, None]) & (j[None, :] < dim[hp["B"]][:, None])
+            hi, lo = np.maximum(fa, fb), np.minimum(fa, fb)
+            idx = np.where(ok, hi * (hi + 1) // 2 + lo, nao2)
+            self._pair_ao = (self.h_pairs, torch.as_tensor(idx.reshape(-1), device=self.dev))
+        # shell pairs in some off-diagonal stored quartet, with no host round trip
+        tv = torch.cat([tasks.view(ntask, 2) for rec in self.classes.values() for tasks, ntask in rec.values()])
+        tv = tv.to(torch.int64)
+        # (plain scatters of True; the diagonal tasks and empty slots go to a sink slot)
+        sink = torch.full_like(tv[:, 0], self.npair)
+        off = tv[:, 0] != tv[:, 1]
+        used = torch.zeros(self.npair + 1, dtype=torch.bool, device=self.dev)
+        used[torch.where(off, tv[:, 0], sink)] = True
+        used[torch.where(off, tv[:, 1], sink)] = True
+        flag = torch.zeros(nao2 + 1, dtype=torch.bool, device=self.dev)
+        idx = self._pair_ao[1]
+        flag[torch.where(used[:self.npair].repeat_interleave(25), idx, torch.full_like(idx, nao2))] = True
+        flag = flag[:nao2]
+        rank = torch.cumsum(flag, 0, dtype=torch.int32)
+        pmap = torch.where(flag, rank - 1, -1).to(torch.int32)
+        return pmap, int(rank[-1])
+
+    def dense_eri_pairs(self, compact=False):
+        """The dense tensor with the bra pair packed: E[pair(a, b)][c][d], a >= b,
+        pair(a, b) = a(a+1)/2 + b (nbf(nbf+1)/2 x nbf x nbf), zero where screened out.
+        compact=True keeps only the AO pairs with rows in stored_pair_map and returns
+        (E (count x nbf x nbf), map, count); it goes through the count x count symmetric
+        pair matrix (two scattered stores per stored element, then one coalesced unpack)."""
+        n = self.nbf
+        if compact:
+            # the rows x rows symmetric pair matrix, then its columns unpacked to (c, d)
+            pmap, rows = self.stored_pair_map()
+            M = torch.zeros(rows * rows, dtype=torch.float64, device=self.dev)
+            for cls, rec in self.classes.items():
+                for part, (tasks, ntask) in rec.items():
+                    _lib.call("pcg_sym_pairs_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
+                              _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), _ptr(pmap), rows, _ptr(M),
+                              _stream())
+            E = torch.empty(rows, n, n, dtype=torch.float64, device=self.dev)
+            _lib.call("pcg_unpack_pairs", rows, n, rows, _ptr(pmap), _ptr(M), _ptr(E), _stream())
+            return E, pmap, rows
+        pmap, rows = None, n * (n + 1) // 2
+        E = torch.zeros(rows * n * n, dtype=torch.float64, device=self.dev)
         for cls, rec in self.classes.items():
             for part, (tasks, ntask) in rec.items():
                 _lib.call("pcg_dense_pairs_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
-                          _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), _ptr(E), _stream())
-        return E.view(n * (n + 1) // 2, n, n)
+                          _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), _ptr(pmap), _ptr(E), _stream())
+        E = E.view(rows, n, n)
+        return (E, pmap, rows) if compact else E
 
     def dense_eri(self):
         """Dense nbf^4 tensor (8-fold symmetric fill), zero where screened out."""

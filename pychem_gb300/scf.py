@@ -20,13 +20,14 @@ RMP2 is the closed-shell form of ``Methods/mp2.py:43-94`` (identical value for R
 the AO->MO transforms run on the tcgen05 tensor cores with FP64 accuracy
 (ozaki_gemm_tc: Ozaki digit slices, every level in one kernel).
 """
+import ctypes
 import math
 import time
 
 import numpy as np
 import torch
 
-from . import eigen
+from . import _lib, eigen
 
 LINEAR_DEPENDENCE = 1.0e-6   # Data/constants.py:34
 
@@ -334,8 +335,10 @@ def _pair_rows(n, dev):
 def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None, timings=None):
     """(ia|jb) from the AO integrals by four quarter transforms, i, a with Co, Cv and
     j, b with Co2, Cv2 (default: the same; different for the opposite-spin block of
-    UMP2).  eri: the dense tensor (n, n, n, n) or the bra-pair-packed one
-    (n(n+1)/2, n, n) of GpuEngine.dense_eri_pairs.
+    UMP2).  eri: the dense tensor (n, n, n, n), the bra-pair-packed one
+    (n(n+1)/2, n, n) of GpuEngine.dense_eri_pairs, or its compact form (E, map, rows)
+    (dense_eri_pairs(compact=True): only the AO pairs some stored quartet contains, so
+    the first two transforms skip the rows that screening leaves zero).
 
     gemm="tc": each transform is one pcg_ozaki_gemm_tc launch (FP64-accurate on the
     tcgen05 tensor cores) contracting the last, contiguous index of its input and
@@ -364,9 +367,12 @@ def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None, timings=
         return torch.matmul(t3, Cv2).reshape(o, v, o2, v2)                # (i a | j b)
     if gemm != "tc":
         raise ValueError("gemm must be 'tc' or 'fp64'")
-    dev = eri.device
     import ctypes
     from . import _lib
+    pmap = None
+    if isinstance(eri, tuple):                       # (E, map, rows) of dense_eri_pairs(compact=True)
+        eri, pmap, npair = eri
+    dev = eri.device
     if eri.dim() == 4:
         eri = eri.reshape(n * n, n * n)[_pair_rows(n, dev)]
     E = eri.reshape(-1)
@@ -387,7 +393,8 @@ def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None, timings=
     T2p = quarter(T1, o * npair, Cv, v)
     del T1
     T2 = torch.empty(v * o * n * n, dtype=torch.float64, device=dev)
-    _lib.call("pcg_unpack_pairs", v * o, n, ctypes.c_void_p(T2p.data_ptr()), ctypes.c_void_p(T2.data_ptr()),
+    _lib.call("pcg_unpack_pairs", v * o, n, npair, ctypes.c_void_p(pmap.data_ptr()) if pmap is not None else None,
+              ctypes.c_void_p(T2p.data_ptr()), ctypes.c_void_p(T2.data_ptr()),
               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     del T2p
     T3 = quarter(T2, v * o * n, Co2, o2)
@@ -407,19 +414,30 @@ def rmp2(engine, C, eps, eri=None, gemm="tc", nslice=6, scale=None):
     mol = engine.mol
     o = mol.NAlphaElectrons
     if eri is None:
-        eri = engine.dense_eri() if gemm == "fp64" else engine.dense_eri_pairs()
+        eri = engine.dense_eri() if gemm == "fp64" else engine.dense_eri_pairs(compact=True)
     Co = C[:, :o].contiguous()
     Cv = C[:, o:].contiguous()
     ovov = mp2_transform(eri, Co, Cv, gemm=gemm, nslice=nslice)
-    eo, ev = eps[:o], eps[o:]
-    den = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
+    s1, s2 = mp2_pair_sums(ovov, eps[:o].contiguous(), eps[o:].contiguous())
     if scale is not None:
-        t = ovov / den
-        e_os = torch.sum(ovov * t)
-        e_ss = torch.sum((ovov - ovov.permute(0, 3, 2, 1)) * t)
-        return float(scale[0] * e_ss + scale[1] * e_os)
-    e2 = torch.sum(ovov * (2.0 * ovov - ovov.permute(0, 3, 2, 1)) / den)
-    return float(e2)
+        return scale[0] * (s1 - s2) + scale[1] * s1        # same spin, opposite spin
+    return 2.0 * s1 - s2
+
+
+def mp2_pair_sums(ovov, eo, ev):
+    """(s1, s2) = (sum (ia|jb)^2 / D, sum (ia|jb)(ib|ja) / D), D = e_i + e_j - e_a - e_b,
+    in one kernel (pcg_mp2_pair_sums) over ovov[i, a, j, b] stored b-major (the layout
+    mp2_transform returns)."""
+    o, v = ovov.shape[0], ovov.shape[1]
+    X = ovov.permute(3, 2, 1, 0)
+    if not X.is_contiguous() or ovov.shape[2] != o or ovov.shape[3] != v:
+        X = ovov.permute(3, 2, 1, 0).contiguous()
+    part = torch.empty(o * v, 2, dtype=torch.float64, device=ovov.device)
+    vp = ctypes.c_void_p
+    _lib.call("pcg_mp2_pair_sums", o, v, vp(X.data_ptr()), vp(eo.data_ptr()), vp(ev.data_ptr()), vp(part.data_ptr()),
+              vp(torch.cuda.current_stream().cuda_stream))
+    s = part.sum(0).tolist()
+    return s[0], s[1]
 
 
 def mp2_flops(n, o, v):
@@ -595,17 +613,15 @@ def ump2(engine, res, eri=None, gemm="tc", nslice=6, scale=None):
     mol = engine.mol
     na, nb = mol.NAlphaElectrons, mol.NBetaElectrons
     if eri is None:
-        eri = engine.dense_eri() if gemm == "fp64" else engine.dense_eri_pairs()
+        eri = engine.dense_eri() if gemm == "fp64" else engine.dense_eri_pairs(compact=True)
     Ca, Cb, ea, eb = res.Ca, res.Cb, res.ea, res.eb
 
     def same(C, e, o):
         if o == 0 or o == C.shape[1]:
             return 0.0
         g = mp2_transform(eri, C[:, :o].contiguous(), C[:, o:].contiguous(), gemm=gemm, nslice=nslice)
-        eo, ev = e[:o], e[o:]
-        den = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
-        t = g - g.permute(0, 3, 2, 1)
-        return 0.25 * float(torch.sum(t * t / den))
+        s1, s2 = mp2_pair_sums(g, e[:o].contiguous(), e[o:].contiguous())
+        return 0.5 * (s1 - s2)           # 0.25 sum ((ia|jb) - (ib|ja))^2 / D
 
     e_ab = 0.0
     if na and nb:

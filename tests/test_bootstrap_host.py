@@ -306,9 +306,10 @@ def test_noci_then_scattering_section(monkeypatch, tmp_path):
 
 
 def _cpu_ump2(eng, res, scale=None):
-    """scf.ump2 on CPU: its FP64 transform over the oracle's dense ERI tensor."""
-    from pychem_gb300.scf import ump2
-    return ump2(eng, res, eri=torch.tensor(eng.eri), gemm="fp64", scale=scale)
+    """scf.ump2's stand-in on CPU: the oracle's UMP2 over its dense ERI tensor."""
+    m = eng.mol
+    return oracle.ump2(*(np.asarray(t.cpu() if hasattr(t, "cpu") else t) for t in (res.Ca, res.Cb, res.ea, res.eb)),
+                       eng.eri, m.NAlphaElectrons, m.NBetaElectrons, scale=scale)
 
 
 with open(os.path.join(HERE, "golden", "mp2_states.json")) as _fh:

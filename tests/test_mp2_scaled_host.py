@@ -1,7 +1,8 @@
 """Spin-component-scaled MP2 (Methods/mp2.py:97-107) on CPU: pychem_gb300.scf.rmp2 /
 ump2 with their FP64 transform path on CPU tensors, from the oracle's SCF orbitals,
 against the reference's MP2, MP2-SCS and MP2-SOS correlation energies
-(make_golden_mp2_scaled.py)."""
+(make_golden_mp2_scaled.py).  The pair-sum kernel (pcg_mp2_pair_sums) is replaced by
+the same sums in torch, so that the host logic around it runs without a GPU."""
 import json
 import os
 
@@ -18,13 +19,21 @@ with open(os.path.join(HERE, "golden", "mp2_scaled.json")) as _fh:
     CASES = json.load(_fh)
 
 
+def _torch_pair_sums(ovov, eo, ev):
+    den = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
+    t = ovov / den
+    return float(torch.sum(ovov * t)), float(torch.sum(ovov.permute(0, 3, 2, 1) * t))
+
+
 class _Eng:
     def __init__(self, mol):
         self.mol = mol
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_scaled_mp2_matches_reference(name):
+def test_scaled_mp2_matches_reference(name, monkeypatch):
+    from pychem_gb300 import scf
+    monkeypatch.setattr(scf, "mp2_pair_sums", _torch_pair_sums)
     case = CASES[name]
     mol = Molecule(case["coords"], case["basis"], multiplicity=case["multiplicity"])
     b = oracle.Basis([(a[0], a[1], *a[2]) for a in mol.atoms], mol.Basis)
