@@ -264,9 +264,17 @@ int pcg_dense_pairs_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *
  * stores. */
 int pcg_sym_pairs_class(int cls, const pcg_basis_t *basis, const pcg_pairs_t *pairs, const int *tasks, int ntask,
                         const double *store, const int *pairmap, long long rows, double *M, void *stream);
-/* out[r][a][b] = in[r * len + pairmap[pair(a, b)]] (0 where pairmap is -1) for r < R,
- * a, b < n: pair-packed rows of length len unpacked (pairmap NULL: the pair itself). */
-int pcg_unpack_pairs(long long R, int n, int len, const int *pairmap, const double *in, double *out, void *stream);
+/* used[p] = 1 (bytes, zeroed by the caller, one per shell pair) for both shell pairs of
+ * every task (x, y) of a class list with x != y: the pairs that some off-diagonal
+ * stored quartet contains (the rows of the compact pair tensor). */
+int pcg_mark_pairs(const int *tasks, int ntask, unsigned char *used, void *stream);
+/* colmap[a*n + b] = pairmap[pair(a, b)] (pairmap NULL: pair(a, b) itself), n x n ints:
+ * where each (a, b) sits in a pair-packed row, -1 for nowhere. */
+int pcg_pair_colmap(int n, const int *pairmap, int *colmap, void *stream);
+/* out[r][a][b] = in[r * len + colmap[a*n + b]] (0 where colmap is -1) for r < R,
+ * a, b < n: pair-packed rows of length len unpacked (colmap from pcg_pair_colmap); a
+ * row of up to 12,800 doubles is staged in shared memory. */
+int pcg_unpack_pairs(long long R, int n, int len, const int *colmap, const double *in, double *out, void *stream);
 
 /* FP64-accurate GEMM with every Ozaki level in one tcgen05 tensor-core kernel (no
  * upstream counterpart; it carries the AO->MO transform of Methods/mp2.py:43-69 and

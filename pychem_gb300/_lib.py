@@ -88,6 +88,8 @@ _SIGS = {
                               c_void_p, c_void_p, c_void_p],
     "pcg_sym_pairs_class": [c_int, ctypes.POINTER(BasisT), ctypes.POINTER(PairsT), c_void_p, c_int, c_void_p,
                             c_void_p, c_longlong, c_void_p, c_void_p],
+    "pcg_mark_pairs": [c_void_p, c_int, c_void_p, c_void_p],
+    "pcg_pair_colmap": [c_int, c_void_p, c_void_p, c_void_p],
     "pcg_unpack_pairs": [c_longlong, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
     "pcg_dgemm": [c_int, c_int, c_int, c_int, c_double, c_void_p, c_longlong, c_longlong, c_longlong, c_void_p,
                   c_longlong, c_longlong, c_longlong, c_double, c_void_p, c_longlong, c_longlong, c_longlong, c_void_p],
@@ -104,7 +106,7 @@ _SIGS = {
 }
 # entry points that launch exactly one kernel of this library per call
 LAUNCHERS = {"pcg_pair_data", "pcg_pair_data_f32", "pcg_pair_ao", "pcg_one_electron", "pcg_eri_class", "pcg_schwarz_class", "pcg_expand_tasks",
-             "pcg_digest_class", "pcg_digest_class_u", "pcg_digest_class_co", "pcg_scattering_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_jacobi_eigh", "pcg_dense_pairs_class", "pcg_sym_pairs_class", "pcg_unpack_pairs",
+             "pcg_digest_class", "pcg_digest_class_u", "pcg_digest_class_co", "pcg_scattering_class", "pcg_fock_build", "pcg_fock_build_batched", "pcg_dense_class", "pcg_fma_probe", "pcg_jacobi_eigh", "pcg_dense_pairs_class", "pcg_sym_pairs_class", "pcg_mark_pairs", "pcg_pair_colmap", "pcg_unpack_pairs",
              "pcg_dgemm", "pcg_oa_correction", "pcg_mp2_pair_sums", "pcg_mlp_gemm", "pcg_mlp_dsilu",
              "pcg_mlp_colsum", "pcg_mlp_mse", "pcg_mlp_adam",
              "pcg_shellpair_quantities", "pcg_two_electron_bound", "pcg_two_electron_fundamentals",

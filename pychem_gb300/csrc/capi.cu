@@ -192,12 +192,28 @@ int pcg_sym_pairs_class(int cls, const pcg_basis_t* basis, const pcg_pairs_t* pa
                               (cudaStream_t)stream);
 }
 
-int pcg_unpack_pairs(long long R, int n, int len, const int* pairmap, const double* in, double* out, void* stream) {
-  if (R < 0 || n < 1 || len < 1 || !in || !out || (!pairmap && len < n * (n + 1) / 2)) {
+int pcg_mark_pairs(const int* tasks, int ntask, unsigned char* used, void* stream) {
+  if (ntask < 0 || !used || (ntask > 0 && !tasks)) {
+    pcg_set_error("pcg_mark_pairs: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  return pcg_launch_mark_pairs((const int2*)tasks, ntask, used, (cudaStream_t)stream);
+}
+
+int pcg_pair_colmap(int n, const int* pairmap, int* colmap, void* stream) {
+  if (n < 1 || n > 46340 || !colmap) {
+    pcg_set_error("pcg_pair_colmap: bad arguments");
+    return PCG_ERR_ARG;
+  }
+  return pcg_launch_pair_colmap(n, pairmap, colmap, (cudaStream_t)stream);
+}
+
+int pcg_unpack_pairs(long long R, int n, int len, const int* colmap, const double* in, double* out, void* stream) {
+  if (R < 0 || n < 1 || n > 46340 || len < 1 || !colmap || !in || !out) {
     pcg_set_error("pcg_unpack_pairs: bad arguments");
     return PCG_ERR_ARG;
   }
-  return pcg_launch_unpack_pairs(R, n, len, pairmap, in, out, (cudaStream_t)stream);
+  return pcg_launch_unpack_rows(R, n, len, colmap, in, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -213,18 +213,47 @@ __global__ void k_sym_pairs(DevBasis b, DevPairsExt pr, const int2* __restrict__
     }
 }
 
-// out[r][a][b] = in[r][map(pair(a, b))] for r < R, a, b < n: rows of `in` have `len`
-// entries; pmap (optional) gives the row position of each pair or -1 for a pair that
-// is not stored (its value is 0); without pmap the position is pair(a, b) itself
-__global__ void k_unpack_pairs(long long R, int n, int len, const int* __restrict__ pmap,
-                               const double* __restrict__ in, double* __restrict__ out) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long nn = (long long)n * n;
-  if (idx >= R * nn) return;
-  const long long r = idx / nn;
-  const int ab = (int)(idx - r * nn), a = ab / n, bb = ab - a * n;
-  const long long q = pmap ? (long long)__ldg(pmap + ao_pair(a, bb)) : (long long)ao_pair(a, bb);
-  out[idx] = q >= 0 ? __ldg(in + r * len + q) : 0.0;
+// used[p] = 1 for both pairs of every task (x, y) with x != y; a byte is read before it
+// is written, so the many tasks of one pair store it once or a few times
+__global__ void k_mark_pairs(const int2* __restrict__ tasks, int ntask, unsigned char* __restrict__ used) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  const int2 tk = tasks[t];
+  if (tk.x == tk.y) return;
+  if (!used[tk.x]) used[tk.x] = 1;
+  if (!used[tk.y]) used[tk.y] = 1;
+}
+
+// colmap[a*n + b] = pmap[pair(a, b)] (pair(a, b) itself without pmap): where each
+// (a, b) of an unpacked row is found in a pair-packed row, -1 for none
+__global__ void k_pair_colmap(int n, const int* __restrict__ pmap, int* __restrict__ colmap) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const int a = idx / n, bb = idx - a * n;
+  const size_t p = ao_pair(a, bb);
+  colmap[idx] = pmap ? pmap[p] : (int)p;
+}
+
+// out[r][ab] = in[r][colmap[ab]] (0 where colmap is -1), one block per row (grid-
+// stride over rows); with SH the packed row is staged in shared memory first, so the
+// gather reads shared memory and both global streams are coalesced
+template <bool SH>
+__global__ void __launch_bounds__(512) k_unpack_rows(long long R, int nn, int len, const int* __restrict__ colmap,
+                                                      const double* __restrict__ in, double* __restrict__ out) {
+  extern __shared__ double row_sh[];
+  for (long long r = blockIdx.x; r < R; r += gridDim.x) {
+    const double* src = in + r * len;
+    if (SH) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < len; q += blockDim.x) row_sh[q] = __ldcs(src + q);
+      __syncthreads();
+    }
+    double* dst = out + r * nn;
+    for (int ab = threadIdx.x; ab < nn; ab += blockDim.x) {
+      const int q = __ldg(colmap + ab);
+      __stcs(dst + ab, q < 0 ? 0.0 : (SH ? row_sh[q] : __ldg(src + q)));
+    }
+  }
 }
 
 int pcg_launch_dense_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
@@ -257,11 +286,30 @@ int pcg_launch_sym_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, cons
   return PCG_OK;
 }
 
-int pcg_launch_unpack_pairs(long long R, int n, int len, const int* pmap, const double* in, double* out,
-                            cudaStream_t s) {
-  const long long total = R * n * n;
-  if (total <= 0) return PCG_OK;
-  k_unpack_pairs<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(R, n, len, pmap, in, out);
+int pcg_launch_mark_pairs(const int2* tasks, int ntask, unsigned char* used, cudaStream_t s) {
+  if (ntask <= 0) return PCG_OK;
+  k_mark_pairs<<<(ntask + 255) / 256, 256, 0, s>>>(tasks, ntask, used);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+int pcg_launch_pair_colmap(int n, const int* pmap, int* colmap, cudaStream_t s) {
+  k_pair_colmap<<<(n * n + 255) / 256, 256, 0, s>>>(n, pmap, colmap);
+  PCG_CUDA(cudaGetLastError());
+  return PCG_OK;
+}
+
+int pcg_launch_unpack_rows(long long R, int n, int len, const int* colmap, const double* in, double* out,
+                           cudaStream_t s) {
+  if (R <= 0) return PCG_OK;
+  const unsigned blocks = (unsigned)(R < 152LL * 64 ? R : 152LL * 64);
+  const size_t sh = (size_t)len * sizeof(double);
+  if (sh <= 100 * 1024) {
+    PCG_CUDA(cudaFuncSetAttribute(k_unpack_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+    k_unpack_rows<true><<<blocks, 512, sh, s>>>(R, n * n, len, colmap, in, out);
+  } else {
+    k_unpack_rows<false><<<blocks, 512, 0, s>>>(R, n * n, len, colmap, in, out);
+  }
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;
 }

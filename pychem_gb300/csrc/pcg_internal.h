@@ -57,8 +57,10 @@ int pcg_launch_dense_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, co
                            const double* store, const int* pmap, double* E, cudaStream_t s);
 int pcg_launch_sym_pairs(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                          const double* store, const int* pmap, long long rows, double* M, cudaStream_t s);
-int pcg_launch_unpack_pairs(long long R, int n, int len, const int* pmap, const double* in, double* out,
-                            cudaStream_t s);
+int pcg_launch_mark_pairs(const int2* tasks, int ntask, unsigned char* used, cudaStream_t s);
+int pcg_launch_pair_colmap(int n, const int* pmap, int* colmap, cudaStream_t s);
+int pcg_launch_unpack_rows(long long R, int n, int len, const int* colmap, const double* in, double* out,
+                           cudaStream_t s);
 int pcg_launch_dense(int cls, const DevBasis& b, const DevPairsExt& pr, const int2* tasks, int ntask,
                      const double* store, double* eri, cudaStream_t s);
 

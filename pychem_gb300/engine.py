@@ -32,6 +32,14 @@ def pair_class(la, lb):
     return la * (la + 1) // 2 + lb
 
 
+def pair_colmap(n, pmap, device):
+    """(n x n int32) where each AO pair (a, b) sits in a pair-packed row: pmap[pair(a, b)]
+    (-1: not stored), or pair(a, b) itself when pmap is None (pcg_pair_colmap)."""
+    cm = torch.empty(n * n, dtype=torch.int32, device=device)
+    _lib.call("pcg_pair_colmap", n, _ptr(pmap), _ptr(cm), _stream())
+    return cm
+
+
 def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32, kind_work=None):
     """Screened canonical quartet plan (Methods/hartree_fock.py:241-312: the quartet
     loop, the Schwarz test Q_ab Q_cd > threshold, and the diagonal quartet that is
@@ -412,8 +420,8 @@ class GpuEngine:
         a 16-water cluster 56 % of the AO pairs have rows."""
         n = self.nbf
         nao2 = n * (n + 1) // 2
-        if getattr(self, "_pair_ao", None) is None or self._pair_ao[0] is not self.h_pairs:
-            # the AO pairs of every shell pair (up to 5 x 5), nao2 where a slot is empty
+        if getattr(self, "_ao_shell_pair", None) is None or self._ao_shell_pair[0] is not self.h_pairs:
+            # the shell pair of every AO pair a >= b
             a, hp = self.h_basis, self.h_pairs
             ao, dim = a["sh_ao"].astype(np.int64), 2 * a["sh_l"].astype(np.int64) + 1
             i, j = np.divmod(np.arange(25), 5)
@@ -421,21 +429,15 @@ class GpuEngine:
             fb = ao[hp["B"]][:, None] + j[None, :]
             ok = (i[None, :] < dim[hp["A"]][:, None]) & (j[None, :] < dim[hp["B"]][:, None])
             hi, lo = np.maximum(fa, fb), np.minimum(fa, fb)
-            idx = np.where(ok, hi * (hi + 1) // 2 + lo, nao2)
-            self._pair_ao = (self.h_pairs, torch.as_tensor(idx.reshape(-1), device=self.dev))
-        # shell pairs in some off-diagonal stored quartet, with no host round trip
-        tv = torch.cat([tasks.view(ntask, 2) for rec in self.classes.values() for tasks, ntask in rec.values()])
-        tv = tv.to(torch.int64)
-        # (plain scatters of True; the diagonal tasks and empty slots go to a sink slot)
-        sink = torch.full_like(tv[:, 0], self.npair)
-        off = tv[:, 0] != tv[:, 1]
-        used = torch.zeros(self.npair + 1, dtype=torch.bool, device=self.dev)
-        used[torch.where(off, tv[:, 0], sink)] = True
-        used[torch.where(off, tv[:, 1], sink)] = True
-        flag = torch.zeros(nao2 + 1, dtype=torch.bool, device=self.dev)
-        idx = self._pair_ao[1]
-        flag[torch.where(used[:self.npair].repeat_interleave(25), idx, torch.full_like(idx, nao2))] = True
-        flag = flag[:nao2]
+            sp = np.empty(nao2, dtype=np.int64)
+            sp[(hi * (hi + 1) // 2 + lo)[ok]] = np.broadcast_to(np.arange(self.npair)[:, None], ok.shape)[ok]
+            self._ao_shell_pair = (self.h_pairs, torch.as_tensor(sp, device=self.dev))
+        # shell pairs in some off-diagonal stored quartet (pcg_mark_pairs), no host round trip
+        used = torch.zeros(self.npair, dtype=torch.bool, device=self.dev)
+        for rec in self.classes.values():
+            for tasks, ntask in rec.values():
+                _lib.call("pcg_mark_pairs", _ptr(tasks), ntask, _ptr(used), _stream())
+        flag = used[self._ao_shell_pair[1]]
         rank = torch.cumsum(flag, 0, dtype=torch.int32)
         pmap = torch.where(flag, rank - 1, -1).to(torch.int32)
         return pmap, int(rank[-1])
@@ -457,7 +459,8 @@ class GpuEngine:
                               _ptr(tasks), ntask, _ptr(self.stores[(cls, part)]), _ptr(pmap), rows, _ptr(M),
                               _stream())
             E = torch.empty(rows, n, n, dtype=torch.float64, device=self.dev)
-            _lib.call("pcg_unpack_pairs", rows, n, rows, _ptr(pmap), _ptr(M), _ptr(E), _stream())
+            _lib.call("pcg_unpack_pairs", rows, n, rows, _ptr(pair_colmap(n, pmap, self.dev)), _ptr(M), _ptr(E),
+                      _stream())
             return E, pmap, rows
         pmap, rows = None, n * (n + 1) // 2
         E = torch.zeros(rows * n * n, dtype=torch.float64, device=self.dev)

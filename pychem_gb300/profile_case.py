@@ -7,7 +7,8 @@ cases:  water16 ((H2O)16 / 6-31G, 208 AO), water8 ((H2O)8, 104 AO), water4 ((H2O
         6-31G, batched), mlp (the learned-guess network on 65,536 pairs), gemm (one
         tensor-core Ozaki GEMM of the first MP2 transform's shape: 77,824 rows of 208
         FP64 values (130 MB, more than L2) times 208 x 80)
-phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2);
+phases: eri (ERI pass), fock (one Fock build), scf (full RHF), mp2 (RHF + MP2),
+        mp2only (one RHF before the repeats, then MP2 alone per repeat);
         scattering (one j0(S r12) grid value at --S: Schwarz pass, quartet plan,
         integral store, contraction with the RHF densities, each timed);
         noci (the CI matrix of C2 / cc-pVDZ spin-flip doubles with CISD, 27
@@ -75,7 +76,7 @@ def gemm_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="water16", choices=sorted(CASES) + ["ensemble", "mlp", "gemm"])
-    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "train", "scattering", "noci", "tc", "codensity"])
+    ap.add_argument("--phase", default="eri", choices=["eri", "fock", "scf", "mp2", "mp2only", "train", "scattering", "noci", "tc", "codensity"])
     ap.add_argument("--S", type=float, default=2.0)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--repeat", type=int, default=1)
@@ -95,10 +96,14 @@ def main():
         return scattering_case(args, mol)
     eng = GpuEngine(mol, precision=args.precision)
     eng.one_electron(); eng.schwarz(); eng.build_tasks(); eng.compute_eris()
+    if args.phase == "mp2only":
+        r0 = rhf(eng)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.repeat):
-        if args.phase == "eri":
+        if args.phase == "mp2only":
+            rmp2(eng, r0.C, r0.eps)
+        elif args.phase == "eri":
             eng.compute_eris()
         elif args.phase == "fock":
             n = eng.nbf
@@ -118,10 +123,14 @@ def ensemble_case(args):
     from .ensemble import EnsembleEngine, rhf_batched
     mols = [Molecule(c, "6-31G") for c in W.ensemble(n=256, seed=2026)]
     eng = EnsembleEngine(mols, precision=args.precision).prepare()
+    if args.phase == "mp2only":
+        r0 = rhf(eng)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.repeat):
-        if args.phase == "eri":
+        if args.phase == "mp2only":
+            rmp2(eng, r0.C, r0.eps)
+        elif args.phase == "eri":
             eng.compute_eris()
         else:
             r = rhf_batched(eng)

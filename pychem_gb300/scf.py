@@ -393,9 +393,10 @@ def mp2_transform(eri, Co, Cv, gemm="tc", nslice=6, Co2=None, Cv2=None, timings=
     T2p = quarter(T1, o * npair, Cv, v)
     del T1
     T2 = torch.empty(v * o * n * n, dtype=torch.float64, device=dev)
-    _lib.call("pcg_unpack_pairs", v * o, n, npair, ctypes.c_void_p(pmap.data_ptr()) if pmap is not None else None,
-              ctypes.c_void_p(T2p.data_ptr()), ctypes.c_void_p(T2.data_ptr()),
-              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    from .engine import pair_colmap
+    cm = pair_colmap(n, pmap, dev)
+    _lib.call("pcg_unpack_pairs", v * o, n, npair, ctypes.c_void_p(cm.data_ptr()), ctypes.c_void_p(T2p.data_ptr()),
+              ctypes.c_void_p(T2.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     del T2p
     T3 = quarter(T2, v * o * n, Co2, o2)
     del T2
