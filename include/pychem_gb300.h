@@ -324,7 +324,8 @@ int pcg_mp2_pair_sums(int o, int v, const double *X, const double *eo, const dou
                       void *stream);
 
 /* Batched symmetric eigensolver (no upstream counterpart; replaces the LAPACK eigh of
- * Methods/hartree_fock.py:172-175,226): parallel cyclic Jacobi, one CTA per matrix.
+ * Methods/hartree_fock.py:172-175,226): parallel cyclic Jacobi, one CTA per matrix
+ * (FP32 above n = 160: a few CTAs, each with a share of V's rows).
  * A: batch x n x n FP64 (read only); w: batch x n eigenvalues (unsorted, matching the
  * columns of V); V: batch x m x m with m = n rounded up to even, FP64 (fp32 = 0,
  * n <= 136) or FP32 (fp32 = 1, n <= 334); V0 (optional, same type/layout as V):

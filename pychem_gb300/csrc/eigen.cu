@@ -8,10 +8,11 @@
 // Frobenius norm falls below tol times the total norm.
 //
 // T = double keeps A (packed) and V in shared memory (n <= 136; used by the batched
-// small-molecule SCF).  T = float keeps packed A in shared memory and V in global
-// memory (n <= 334 with 227 KB of shared memory); the caller refines the float result in FP64
-// (Ogita-Aishima iteration, pychem_gb300/eigen.py), so the O(n^3) rotation work runs
-// on the FP32 pipe.
+// small-molecule SCF).  T = float (n <= 334) keeps packed A and V in shared memory
+// too, V's rows spread over as many CTAs per matrix as that takes (two at n = 208,
+// eight at n = 298); the caller refines the float result in FP64 (Ogita-Aishima
+// iteration, pychem_gb300/eigen.py), so the O(n^3) rotation work runs on the FP32
+// pipe.
 #include <math.h>
 
 #include "../../include/pychem_gb300.h"
@@ -38,22 +39,32 @@ __device__ __forceinline__ int sym(int i, int j) { return i >= j ? tri(i, j) : t
 // the n/2 rotations, then transforms every 2x2 block (pair k rows, pair k' columns,
 // k >= k') as B' = J_k^T B J_k' -- blocks are disjoint, so one pass suffices -- and
 // the rows of V as V J.
-template <typename T, bool V_SMEM>
-__global__ void k_jacobi(int n, int m, const double* __restrict__ Ain, long long sA, T* __restrict__ Vg, long long sV,
-                         const T* __restrict__ V0, double* __restrict__ w, long long sw, int max_sweeps, double tol,
-                         int* __restrict__ info) {
+//
+// One matrix may be spread over `split` CTAs: every CTA holds the whole packed A and
+// applies the same rotations to it (the same arithmetic in the same order, so the
+// copies stay identical and need no communication), and rows [r0, r1) of V, in shared
+// memory; rotations act on each row of V separately.  That keeps V out of global
+// memory for n up to 334 in FP32.  With use_tab, the (k, k2) pair of every 2x2 block
+// is read from a table in shared memory (after V) instead of being decoded with a
+// square root per block and round.  Rotations that are the identity (a_pq = 0) skip
+// their updates.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_jacobi(int n, int m, int split, int rows_per, const double* __restrict__ Ain,
+                                                 long long sA, T* __restrict__ Vg, long long sV,
+                                                 const T* __restrict__ V0, double* __restrict__ w, long long sw,
+                                                 int max_sweeps, double tol, int* __restrict__ info, int use_tab) {
   extern __shared__ unsigned char smem_raw[];
   T* A = (T*)smem_raw;
   const int ntri = m * (m + 1) / 2;
-  T* V = V_SMEM ? A + ((ntri + 1) & ~1) : Vg + (size_t)blockIdx.x * sV;
-  // rotation tables: m/2 entries (m <= 136 for the shared-memory variant, whose
-  // dynamic part then leaves room for only a few KB of static shared memory)
-  constexpr int HMAX = V_SMEM ? 128 : 512;
+  const int b = blockIdx.x / split, part = blockIdx.x % split;
+  const int r0 = part * rows_per, r1 = min(m, r0 + rows_per), nrow = max(0, r1 - r0);
+  T* V = A + ((ntri + 1) & ~1);                      // rows r0..r1 of V (nrow x m)
+  unsigned* tab = (unsigned*)(V + (((size_t)rows_per * m + 1) & ~(size_t)1));
+  constexpr int HMAX = 176;                          // m / 2 <= 167
   __shared__ T cs[HMAX], sn[HMAX];
   __shared__ int pp[HMAX], qq[HMAX];
   __shared__ double red0[32], red1[32];
   __shared__ int stop;
-  const int b = blockIdx.x;
   const double* Ab = Ain + (size_t)b * sA;
   const int nt = blockDim.x, tid = threadIdx.x;
   for (int idx = tid; idx < ntri; idx += nt) {
@@ -63,16 +74,19 @@ __global__ void k_jacobi(int n, int m, const double* __restrict__ Ain, long long
     const int j = idx - tri(i, 0);
     A[idx] = (i < n && j < n) ? (T)Ab[(size_t)i * n + j] : (T)0;
   }
-  for (int idx = tid; idx < m * m; idx += nt) {
-    const int i = idx / m, j = idx % m;
+  for (int idx = tid; idx < nrow * m; idx += nt) {
+    const int i = r0 + idx / m, j = idx % m;
     T v = (T)(i == j);
-    if (V0 && i < n && j < n) v = V0[(size_t)b * sV + idx];
+    if (V0 && i < n && j < n) v = V0[(size_t)b * sV + (size_t)i * m + j];
     V[idx] = v;
   }
   if (tid == 0) stop = 0;
-  __syncthreads();
   const int h = m / 2;
   const int nblk = h * (h + 1) / 2;
+  if (use_tab)
+    for (int k = tid; k < h; k += nt)
+      for (int k2 = 0; k2 <= k; ++k2) tab[k * (k + 1) / 2 + k2] = ((unsigned)k << 16) | (unsigned)k2;
+  __syncthreads();
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     double off = 0.0, tot = 0.0;
@@ -109,14 +123,21 @@ __global__ void k_jacobi(int n, int m, const double* __restrict__ Ain, long long
         pp[k] = p; qq[k] = q; cs[k] = c; sn[k] = s;
       }
       __syncthreads();
-      for (int it = tid; it < nblk + m * h; it += nt) {
+      for (int it = tid; it < nblk + nrow * h; it += nt) {
         if (it < nblk) {
-          int k = (int)((sqrtf(8.0f * it + 1.0f) - 1.0f) * 0.5f);
-          while ((k + 1) * (k + 2) / 2 <= it) ++k;
-          while (k * (k + 1) / 2 > it) --k;
-          const int k2 = it - k * (k + 1) / 2;  // k >= k2
+          int k, k2;  // k >= k2
+          if (use_tab) {
+            const unsigned e = tab[it];
+            k = (int)(e >> 16); k2 = (int)(e & 0xFFFFu);
+          } else {
+            k = (int)((sqrtf(8.0f * it + 1.0f) - 1.0f) * 0.5f);
+            while ((k + 1) * (k + 2) / 2 <= it) ++k;
+            while (k * (k + 1) / 2 > it) --k;
+            k2 = it - k * (k + 1) / 2;
+          }
           const int p = pp[k], q = qq[k], p2 = pp[k2], q2 = qq[k2];
           const T c = cs[k], s = sn[k], c2 = cs[k2], s2 = sn[k2];
+          if (s == (T)0 && s2 == (T)0) continue;   // both rotations the identity
           if (k == k2) {
             const T app = A[tri(p, p)], aqq = A[tri(q, q)], apq = A[tri(q, p)];
             // J^T [[app, apq], [apq, aqq]] J with the rotation that zeroes apq
@@ -137,9 +158,10 @@ __global__ void k_jacobi(int n, int m, const double* __restrict__ Ain, long long
           }
         } else {
           const int t = it - nblk;
-          const int i = t / h, k = t % h;
-          const int p = pp[k], q = qq[k];
+          const int i = t / h, k = t % h;            // local row i of V
           const T c = cs[k], s = sn[k];
+          if (s == (T)0) continue;
+          const int p = pp[k], q = qq[k];
           const T vp = V[i * m + p], vq = V[i * m + q];
           V[i * m + p] = c * vp - s * vq;
           V[i * m + q] = s * vp + c * vq;
@@ -148,10 +170,30 @@ __global__ void k_jacobi(int n, int m, const double* __restrict__ Ain, long long
       __syncthreads();
     }
   }
-  for (int i = tid; i < n; i += nt) w[(size_t)b * sw + i] = (double)A[tri(i, i)];
-  if (V_SMEM)
-    for (int idx = tid; idx < m * m; idx += nt) Vg[(size_t)b * sV + idx] = V[idx];
-  if (tid == 0 && info) info[b] = sweep;
+  if (part == 0) {
+    for (int i = tid; i < n; i += nt) w[(size_t)b * sw + i] = (double)A[tri(i, i)];
+    if (tid == 0 && info) info[b] = sweep;
+  }
+  for (int idx = tid; idx < nrow * m; idx += nt) Vg[(size_t)b * sV + (size_t)r0 * m + idx] = V[idx];
+}
+
+// shared-memory plan of one launch: how many CTAs share a matrix, rows of V per CTA,
+// whether the block table fits, and the dynamic bytes
+template <typename T>
+static bool jacobi_plan(int m, int& split, int& rows_per, int& tab, size_t& bytes) {
+  const size_t limit = 232448 - 5120;                // 227 KB less the static tables
+  const size_t a_bytes = (size_t)((m * (m + 1) / 2 + 1) & ~1) * sizeof(T);
+  const size_t tab_bytes = (size_t)(m / 2) * (m / 2 + 1) / 2 * sizeof(unsigned);
+  for (split = 1; split <= m; ++split) {
+    rows_per = (m + split - 1) / split;
+    const size_t v_bytes = (size_t)(((size_t)rows_per * m + 1) & ~(size_t)1) * sizeof(T);
+    if (a_bytes + v_bytes <= limit) {
+      tab = a_bytes + v_bytes + tab_bytes <= limit;
+      bytes = a_bytes + v_bytes + (tab ? tab_bytes : 0);
+      return true;
+    }
+  }
+  return false;
 }
 
 extern "C" int pcg_jacobi_eigh(int batch, int n, const double* A, double* w, void* V, int fp32, const void* V0,
@@ -171,34 +213,27 @@ extern "C" int pcg_jacobi_eigh(int batch, int n, const double* A, double* w, voi
     }
   }
   const long long sA = (long long)n * n, sV = (long long)m * m, sw = n;
+  // above n = 64 one CTA per SM is resident anyway (shared memory): 1024 threads
+  const int threads = m <= 32 ? 128 : (m <= 64 ? 256 : 1024);
+  int split = 1, rows_per = m, tab = 0;
+  size_t bytes = 0;
   if (!fp32) {
-    const size_t smem = ((size_t)(m * (m + 1) / 2 + 1) / 2 * 2 + (size_t)m * m) * sizeof(double);
-    if (smem > 220 * 1024 || m / 2 > 128) {
+    if (m / 2 > 68 || !jacobi_plan<double>(m, split, rows_per, tab, bytes) || split != 1) {
       pcg_set_error("pcg_jacobi_eigh: FP64 variant needs n <= 136");
       return PCG_ERR_UNSUPPORTED;
     }
-    const int threads = m <= 32 ? 128 : 256;
-    // opt in to the exact dynamic size: dynamic + static (3.5 KB) may exceed the
-    // 48 KB default even when the dynamic part alone does not
-    PCG_CUDA(cudaFuncSetAttribute(k_jacobi<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_jacobi<double, true><<<batch, threads, smem, s>>>(n, m, A, sA, (double*)V, sV, (const double*)V0, w, sw,
-                                                         max_sweeps, tol, info);
+    PCG_CUDA(cudaFuncSetAttribute(k_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    k_jacobi<double><<<batch, threads, bytes, s>>>(n, m, 1, m, A, sA, (double*)V, sV, (const double*)V0, w, sw,
+                                                   max_sweeps, tol, info, tab);
   } else {
-    // FP32: packed A and V both in shared memory while they fit (n <= 182), else V
-    // in global memory (n <= 334)
-    const size_t smem_v = ((size_t)(m * (m + 1) / 2 + 1) / 2 * 2 + (size_t)m * m) * sizeof(float);
-    if (smem_v <= 200 * 1024 && m / 2 <= 128) {
-      const int threads = m <= 32 ? 128 : 256;
-      PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_v));
-      k_jacobi<float, true><<<batch, threads, smem_v, s>>>(n, m, A, sA, (float*)V, sV, (const float*)V0, w, sw,
-                                                            max_sweeps, tol, info);
-    } else {
-      const size_t smem = (size_t)m * (m + 1) / 2 * sizeof(float);
-      if (smem > 220 * 1024) { pcg_set_error("pcg_jacobi_eigh: FP32 variant needs n <= 334"); return PCG_ERR_UNSUPPORTED; }
-      PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_jacobi<float, false><<<batch, 1024, smem, s>>>(n, m, A, sA, (float*)V, sV, (const float*)V0, w, sw,
-                                                        max_sweeps, tol, info);
+    if (m / 2 > 167 || !jacobi_plan<float>(m, split, rows_per, tab, bytes)) {
+      pcg_set_error("pcg_jacobi_eigh: FP32 variant needs n <= 334");
+      return PCG_ERR_UNSUPPORTED;
     }
+    if ((long long)batch * split > 0x7fffffffLL) { pcg_set_error("pcg_jacobi_eigh: batch too large"); return PCG_ERR_ARG; }
+    PCG_CUDA(cudaFuncSetAttribute(k_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    k_jacobi<float><<<batch * split, threads, bytes, s>>>(n, m, split, rows_per, A, sA, (float*)V, sV,
+                                                          (const float*)V0, w, sw, max_sweeps, tol, info, tab);
   }
   PCG_CUDA(cudaGetLastError());
   return PCG_OK;

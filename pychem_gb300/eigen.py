@@ -174,31 +174,165 @@ def _split_point(w, n, base=EXACT_BLOCK):
 
 def exact_eigh(A, X_prev=None, steps=4):
     """Eigenpairs of one symmetric A to FP64 accuracy on the library's kernels, by
-    spectrum slicing: n <= 64, the FP64 Jacobi kernel (one CTA: its cost grows as n^3
-    on the thin FP64 pipe) started from the FP32 Jacobi vectors (so it needs few
-    sweeps); larger n, the FP32 Jacobi vectors (from X_prev
-    when given), a split at the largest gap that keeps both parts at most 64 (or in
-    the middle half), projector
-    refinement that decouples the two invariant subspaces in FP64, and the same on
-    each part's projected matrix.  Near-degenerate clusters end up inside one part,
-    where Jacobi resolves them."""
-    n = A.shape[-1]
-    if n <= EXACT_BLOCK:
-        _, V32 = eigh32_own(A, X_prev)
-        V = orthonormalize(V32)
-        Ap = dense.mm(V, dense.mm(A, V), ta=True)
-        w, U = jacobi(0.5 * (Ap + Ap.T))
-        return _sort(w, dense.mm(V, U))
-    w32, V = eigh32_own(A, X_prev)
-    s = _split_point(w32, n)
-    _, V = refine_projector(A, V, s, steps=steps)
-    out_w, out_V = [], []
-    for blk in (V[:, :s], V[:, s:]):
+    spectrum slicing (exact_eigh_many with one matrix)."""
+    return exact_eigh_many([A], [X_prev], steps=steps)[0]
+
+
+def _padded(mats, m):
+    """(len(mats), m, m) with each matrix in the top-left corner and, below it, a
+    diagonal of one value above every spectrum: the padding rows are exact, decoupled
+    eigenvectors that sort last and that the Jacobi kernel never rotates."""
+    # one above the largest Gershgorin upper bound (not far above it: the padding adds
+    # to the norm that the Jacobi kernel's stopping test is relative to)
+    big = max(float((torch.diagonal(a) + a.abs().sum(dim=1) - torch.diagonal(a).abs()).amax()) for a in mats) + 1.0
+    out = torch.zeros(len(mats), m, m, dtype=torch.float64, device=mats[0].device)
+    for k, a in enumerate(mats):
+        n = a.shape[0]
+        out[k, :n, :n] = a
+        if n < m:
+            out[k, n:, n:].diagonal().fill_(big)
+    return out
+
+
+def exact_eigh_many(As, X_prevs=None, steps=4):
+    """Eigenpairs of several symmetric matrices to FP64 accuracy, by spectrum slicing,
+    with every Jacobi stage one batched launch (one CTA or a few per matrix, all
+    matrices side by side on the GPU):
+
+    * FP32 Jacobi vectors for every matrix (from X_prev when given);
+    * a matrix above 64 is split at the largest gap that keeps both parts at most 64
+      (or in the middle half), projector refinement decouples the two invariant
+      subspaces in FP64, and each part's projected matrix -- nearly diagonal already,
+      in the FP32 vectors' basis, its diagonal ordering the part's spectrum -- is
+      split the same way while above 64;
+    * every part of at most 64 is finished by the FP64 Jacobi kernel, which needs
+      few sweeps from nearly diagonal, all parts in one batched launch.
+
+    Near-degenerate clusters end up inside one part, where Jacobi resolves them.
+    Returns [(w ascending, V)] in the order of As."""
+    if X_prevs is None:
+        X_prevs = [None] * len(As)
+    roots = []
+    for A, Xp in zip(As, X_prevs):
+        A = A.to(torch.float64)
+        if Xp is not None:
+            Xp = Xp.to(torch.float64)
+            Ab = dense.mm(Xp, dense.mm(A, Xp), ta=True)
+            roots.append((0.5 * (Ab + Ab.T), Xp))
+        else:
+            roots.append((A, None))
+    m = max(a.shape[0] for a, _ in roots)
+    m += m & 1
+    w32, V32 = _jacobi(_padded([a for a, _ in roots], m), True, 12, 1e-5)
+    w32, V32 = _sort(w32, V32.to(torch.float64))
+    # (root, matrix, its columns' basis in the root's space or None, ascending
+    # spectrum estimate, vectors of the estimate in the matrix's space)
+    todo = []
+    for r, (a, B) in enumerate(roots):
+        n = a.shape[0]
+        V = V32[r, :n, :n]
+        if n <= EXACT_BLOCK:
+            V = orthonormalize(V)       # FP32-orthonormal -> FP64 (parts get it from refinement)
+        todo.append((r, a, B, w32[r, :n], V))
+    leaves = []
+    while todo:
+        r, a, B, w, V = todo.pop()
+        n = a.shape[0]
+        if n <= EXACT_BLOCK:
+            # the part in the basis V, where it is nearly diagonal
+            Ap = dense.mm(V, dense.mm(a, V), ta=True)
+            leaves.append((r, 0.5 * (Ap + Ap.T), V if B is None else dense.mm(B, V)))
+            continue
+        s = _split_point(w, n)
+        _, V = refine_projector(a, V, s, steps=steps)
+        for blk in (V[:, :s], V[:, s:]):
+            Ab = dense.mm(blk, dense.mm(a, blk), ta=True)
+            Ab = 0.5 * (Ab + Ab.T)
+            d, order = torch.sort(torch.diagonal(Ab))
+            I = torch.eye(Ab.shape[0], dtype=torch.float64, device=Ab.device)[:, order].contiguous()
+            todo.append((r, Ab, blk if B is None else dense.mm(B, blk), d, I))
+    m = max(a.shape[0] for _, a, _ in leaves)
+    m += m & 1
+    w64, U64 = _jacobi(_padded([a for _, a, _ in leaves], m), False, 40, None)
+    parts = [([], []) for _ in As]
+    for k, (r, a, B) in enumerate(leaves):
+        n = a.shape[0]
+        parts[r][0].append(w64[k, :n])
+        parts[r][1].append(dense.mm(B, U64[k, :n, :n].contiguous()))
+    return [_sort(torch.cat(wl), torch.cat(vl, dim=1)) for wl, vl in parts]
+
+
+def purify(A, nocc, max_iter=120, tol=1e-12):
+    """Projector onto the eigenvectors of the nocc lowest eigenvalues of symmetric A,
+    by canonical purification (A. H. R. Palser and D. E. Manolopoulos, Phys. Rev. B 58
+    (1998) 12704): P0 = lam/n (mu I - A) + nocc/n I with mu = tr(A)/n and lam from
+    Gershgorin bounds of the spectrum, then, with c = tr(P^2 - P^3) / tr(P - P^2),
+    P <- ((1 + c) P^2 - P^3) / c for c >= 1/2, else ((1 - 2c) P + (1 + c) P^2 - P^3) /
+    (1 - c).  The trace stays nocc and P converges to idempotency (quadratically at
+    the end); the step coefficients are formed on the device and the host reads the
+    idempotency error every fourth step.  FP64, library GEMMs."""
+    n = A.shape[0]
+    dev = A.device
+    I = torch.eye(n, dtype=torch.float64, device=dev)
+    d = torch.diagonal(A)
+    r = A.abs().sum(dim=1) - d.abs()
+    emin, emax = torch.min(d - r), torch.max(d + r)
+    mu = torch.trace(A) / n
+    lam = torch.minimum(nocc / (emax - mu), (n - nocc) / (mu - emin))
+    P = (lam / n) * (mu * I - A) + (nocc / n) * I
+    P2 = torch.empty_like(P)
+    P3 = torch.empty_like(P)
+    for it in range(max_iter):
+        dense.mm(P, P, out=P2)
+        dense.mm(P2, P, out=P3)
+        t1, t2, t3 = torch.trace(P), torch.trace(P2), torch.trace(P3)
+        den = t1 - t2
+        c = torch.where(den.abs() > 1e-300, (t2 - t3) / torch.where(den.abs() > 1e-300, den, 1.0), 0.5)
+        ge = c >= 0.5
+        ca = torch.where(ge, 0.0, (1.0 - 2.0 * c) / (1.0 - c))
+        cb = torch.where(ge, (1.0 + c) / c, (1.0 + c) / (1.0 - c))
+        cg = torch.where(ge, -1.0 / c, -1.0 / (1.0 - c))
+        P = ca * P + cb * P2 + cg * P3
+        if it % 4 == 3 and float(den) < tol * n:
+            break
+    return 0.5 * (P + P.T)
+
+
+def rotate_blocks(A, V, cuts, tol=1e-4, max_sweeps=5):
+    """V with each column block [cuts[k], cuts[k+1]) rotated to the FP32 Jacobi
+    eigenvectors of its projected block V_k^T A V_k, every block in one batched
+    launch; the blocks' spans are unchanged and each block of X^T A X becomes
+    nearly diagonal, which projector refinement needs to converge quadratically."""
+    blks = [V[:, a:b] for a, b in zip(cuts[:-1], cuts[1:])]
+    mats = []
+    for blk in blks:
         Ab = dense.mm(blk, dense.mm(A, blk), ta=True)
-        wb, Ub = exact_eigh(0.5 * (Ab + Ab.T))
-        out_w.append(wb)
-        out_V.append(dense.mm(blk, Ub))
-    return _sort(torch.cat(out_w), torch.cat(out_V, dim=1))
+        mats.append(0.5 * (Ab + Ab.T))
+    m = max(a.shape[0] for a in mats)
+    m += m & 1
+    w, U = _jacobi(_padded(mats, m), True, max_sweeps, tol)
+    w, U = _sort(w, U.to(torch.float64))
+    return torch.cat([dense.mm(blk, U[k, :a.shape[0], :a.shape[0]].contiguous())
+                      for k, (blk, a) in enumerate(zip(blks, mats))], dim=1)
+
+
+def projector_basis(P, nocc, seed=0):
+    """An orthonormal basis (n x n) whose first nocc columns span the range of the
+    projector P and the rest its complement: each block from a seeded Gaussian matrix
+    projected (P G, (I - P) G), orthonormalised by Y (Y^T Y)^-1/2 (coupled
+    Newton-Schulz), projected and orthonormalised once more."""
+    n = P.shape[0]
+    g = torch.Generator(device=P.device).manual_seed(seed)
+    G = torch.randn(n, n, dtype=torch.float64, device=P.device, generator=g)
+    out = []
+    for Y, occ in ((G[:, :nocc], True), (G[:, nocc:], False)):
+        for _ in range(2):
+            PY = dense.mm(P, Y)
+            Y = PY if occ else Y - PY
+            Z, _ = dense.inv_sqrt(dense.mm(Y, Y, ta=True))
+            Y = dense.mm(Y, Z)
+        out.append(Y)
+    return torch.cat(out, dim=1).contiguous()
 
 
 def eigh(A, X_prev=None, refine_steps=2, exact=True, check_tol=1e-10, nocc=None):

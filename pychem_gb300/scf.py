@@ -172,11 +172,11 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
             mm(C[:, :nocc], C[:, :nocc], tb=True, out=D)
         mm(Q[:, :nocc], Q[:, :nocc], tb=True, out=Dp)
 
-    def diag_exact(sweeps=5):
+    def diag_exact():
         if big:
             # a few FP32 Jacobi sweeps put the occupied space well inside the HOMO-LUMO
             # gap; the projector refinement does the rest in FP64
-            _, V = eigen.eigh32_own(Fx, Q if have_q[0] else None, tol=1e-4, max_sweeps=sweeps)
+            _, V = eigen.eigh32_own(Fx, Q if have_q[0] else None, tol=1e-4, max_sweeps=5)
             _, V = eigen.refine_projector(Fx, V, nocc, steps=3)
         else:
             _, V = eigen.eigh(Fx, X_prev=Q if have_q[0] else None)
@@ -193,6 +193,10 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
     per_replay = 0
     E_old = None
     history = []
+    phases = {}
+    if record:
+        torch.cuda.synchronize()
+        phases["setup"] = time.perf_counter()
     fallbacks = 0
     t_last = time.perf_counter()
     converged = False
@@ -220,6 +224,8 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
             g.replay()
             _lib_add_launches(per_replay)
         host = vals.cpu().numpy()
+        if record and it <= 2:
+            phases["iteration%d" % it] = time.perf_counter()
         E = float(host[0]) + e_nuc
         if not exact:
             if scale is None:
@@ -242,7 +248,7 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                         ok = True
                         break
                 if not ok:
-                    diag_exact(sweeps=12)
+                    diag_exact()
                 density()
         if E_old is not None:
             drms = float(host[1])
@@ -259,21 +265,25 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
     # clusters) for MP2's denominators: for n > 136 the occupied and virtual blocks of
     # the refined vectors are decoupled once more and each block is diagonalised
     # exactly (spectrum slicing inside blocks above 136)
+    if record:
+        torch.cuda.synchronize()
+        phases["loop"] = time.perf_counter()
     Ff = mm(X, mm(F, X), ta=True)
     if big:
         _, V = eigen.refine_projector(Ff, Q, nocc, steps=2)
-        ws, Vs = [], []
-        for blk in (V[:, :nocc], V[:, nocc:]):
-            Ab = mm(blk, mm(Ff, blk), ta=True)
-            wb, Ub = eigen.exact_eigh(0.5 * (Ab + Ab.T))
-            ws.append(wb)
-            Vs.append(mm(blk, Ub))
-        eps, Qf = torch.cat(ws), torch.cat(Vs, dim=1)
+        blks = (V[:, :nocc], V[:, nocc:])
+        Abs = [mm(blk, mm(Ff, blk), ta=True) for blk in blks]
+        res = eigen.exact_eigh_many([0.5 * (Ab + Ab.T) for Ab in Abs])
+        eps = torch.cat([wb for wb, _ in res])
+        Qf = torch.cat([mm(blk, Ub) for blk, (_, Ub) in zip(blks, res)], dim=1)
     else:
         eps, Qf = eigen.eigh(Ff, exact=True)
     Cf = mm(X, Qf)
     Dn = mm(Cf[:, :nocc], Cf[:, :nocc], tb=True)
-    return SCFResult(E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=Cf, eps=eps, D=Dn, F=F, iterations=it,
+    if record:
+        torch.cuda.synchronize()
+        phases["final"] = time.perf_counter()
+    return SCFResult(phases=phases, E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=Cf, eps=eps, D=Dn, F=F, iterations=it,
                      converged=converged, history=history, fock_builds=it, diag_fallbacks=fallbacks)
 
 
