@@ -1,9 +1,9 @@
 // Small dense FP64 algebra of the SCF iteration, all on the GPU:
 //
 //  * pcg_dgemm: batched C = alpha A B + beta C with arbitrary element strides (so any
-//    transposes), 16 x 16 output tiles of one thread per element.  GB300's FP64 pipe
+//    transposes), 8 x 8 output tiles of one thread per element.  GB300's FP64 pipe
 //    is thin (about 1.7 FMA per clock per SM), so the SCF's n <= 300 products are
-//    spread over as many CTAs as possible: 169 for n = 208.  Replaces the numpy.dot /
+//    spread over many CTAs: 676 for n = 208.  Replaces the numpy.dot /
 //    matrix products of Methods/hartree_fock.py:168-184 and
 //    Methods/hf_extensions/diis.py:48-54 (X^T F X, the commutator, C = X C').
 //  * pcg_oa_correction: the correction matrix of one Ogita-Aishima refinement step of
@@ -20,27 +20,36 @@
 #include "common.cuh"
 #include "pcg_internal.h"
 
-#define DG_T 16
+// 8 x 8 output tiles (one thread per element), K in steps of 32: at n = 208 that is
+// 676 CTAs, 4-5 per SM, so the FP64 work is spread evenly over the 152 SMs (with
+// 16 x 16 tiles the 169 CTAs left 17 SMs with twice the work of the others).
+#define DG_T 8
+#define DG_K 32
 
 __global__ void __launch_bounds__(DG_T* DG_T)
     k_dgemm(int M, int N, int K, double alpha, const double* __restrict__ A, long long sAb, long long sAm,
             long long sAk, const double* __restrict__ B, long long sBb, long long sBk, long long sBn, double beta,
             double* __restrict__ C, long long sCb, long long sCm, long long sCn) {
-  __shared__ double As[DG_T][DG_T + 1], Bs[DG_T][DG_T + 1];
-  const int tx = threadIdx.x % DG_T, ty = threadIdx.x / DG_T;
+  __shared__ double As[DG_T][DG_K + 1], Bs[DG_K][DG_T + 1];
+  const int tid = threadIdx.x, tx = tid % DG_T, ty = tid / DG_T;
   const long long b = blockIdx.z;
-  const int m = blockIdx.y * DG_T + ty, n = blockIdx.x * DG_T + tx;
+  const int m0 = blockIdx.y * DG_T, n0 = blockIdx.x * DG_T;
+  const int m = m0 + ty, n = n0 + tx;
   A += b * sAb;
   B += b * sBb;
   double acc = 0.0;
-  for (int k0 = 0; k0 < K; k0 += DG_T) {
-    const int ka = k0 + tx;
-    As[ty][tx] = (m < M && ka < K) ? __ldg(A + m * sAm + ka * sAk) : 0.0;
-    const int kb = k0 + ty;
-    Bs[ty][tx] = (kb < K && n < N) ? __ldg(B + kb * sBk + n * sBn) : 0.0;
+  for (int k0 = 0; k0 < K; k0 += DG_K) {
+#pragma unroll
+    for (int e = tid; e < DG_T * DG_K; e += DG_T * DG_T) {
+      const int r = e / DG_K, kk = e % DG_K;
+      const int mr = m0 + r, ka = k0 + kk;
+      As[r][kk] = (mr < M && ka < K) ? __ldg(A + mr * sAm + ka * sAk) : 0.0;
+      const int kb = k0 + e / DG_T, c = n0 + e % DG_T;
+      Bs[e / DG_T][e % DG_T] = (kb < K && c < N) ? __ldg(B + kb * sBk + c * sBn) : 0.0;
+    }
     __syncthreads();
 #pragma unroll
-    for (int kk = 0; kk < DG_T; ++kk) acc = fma(As[ty][kk], Bs[kk][tx], acc);
+    for (int kk = 0; kk < DG_K; ++kk) acc = fma(As[ty][kk], Bs[kk][tx], acc);
     __syncthreads();
   }
   if (m < M && n < N) {

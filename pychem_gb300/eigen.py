@@ -132,7 +132,7 @@ def refine(A, X, steps=2):
     return lam.clone(), X
 
 
-def refine_projector(A, X, nocc, steps=2, check=False):
+def refine_projector(A, X, nocc, steps=2, check=False, ortho_steps=1):
     """Refinement that only decouples the first nocc columns (occupied) from the rest
     (virtual): Ogita-Aishima corrections for occupied-virtual pairs, separated by at
     least the HOMO-LUMO gap, and re-orthonormalisation (E = R/2) inside each block, so
@@ -148,8 +148,8 @@ def refine_projector(A, X, nocc, steps=2, check=False):
         E = dense.oa_correction(S, R, nocc, 0, lam=lam)
         X = _step(X, E)
     # the occupied-virtual rotations of large steps leave O(E^2) non-orthogonality;
-    # one Newton-Schulz step X <- X + X (I - X^T X)/2 removes it quadratically
-    X = orthonormalize(X, steps=1)
+    # a Newton-Schulz step X <- X + X (I - X^T X)/2 removes it quadratically
+    X = orthonormalize(X, steps=ortho_steps)
     if not check:
         return lam, X
     R, S = _rs(A, X)

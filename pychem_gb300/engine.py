@@ -275,8 +275,12 @@ class GpuEngine:
         Q = torch.zeros(self.npair, dtype=torch.float64, device=self.dev)
         pc = pair_class(self.h_pairs["lA"], self.h_pairs["lB"])
         self.diag_blocks = {}
+        npp = self.h_pairs["npp"]
         for c in np.unique(pc):
             ids = np.nonzero(pc == c)[0].astype(np.int32)
+            # heaviest pairs first: the warps run uniform primitive loops and the long
+            # quartets start early
+            ids = ids[np.argsort(-npp[ids], kind="stable")]
             la, lb = int(self.h_pairs["lA"][ids[0]]), int(self.h_pairs["lB"][ids[0]])
             cls = _lib.load().pcg_eri_class_id(la, lb, la, lb)
             tasks = self._t(np.stack([ids, ids], axis=1))
@@ -325,16 +329,25 @@ class GpuEngine:
         self._task_stats()
         return self.classes
 
+    @property
+    def prim_quartets(self):
+        """Primitive quartets per (class, part) of the current task lists (for the
+        algorithmic flop count), computed on first use after build_tasks."""
+        if self._prim_quartets is None:
+            self._prim_quartets = {}
+            npp = self.pd["npp"].to(torch.int64)
+            for cls, rec in self.classes.items():
+                for part, (tasks, n) in rec.items():
+                    tv = tasks.view(n, 2).to(torch.int64)
+                    self._prim_quartets[(cls, part)] = (npp[tv[:, 0]] * npp[tv[:, 1]]).sum()
+        return self._prim_quartets
+
+    _prim_quartets = None
+
     def _task_stats(self):
         nq64 = sum(rec["64"][1] for rec in self.classes.values() if "64" in rec)
         nq32 = sum(rec["32"][1] for rec in self.classes.values() if "32" in rec)
-        # primitive quartets per class and part (for the algorithmic flop count)
-        self.prim_quartets = {}
-        npp = self.pd["npp"].to(torch.int64)
-        for cls, rec in self.classes.items():
-            for part, (tasks, n) in rec.items():
-                tv = tasks.view(n, 2).to(torch.int64)
-                self.prim_quartets[(cls, part)] = (npp[tv[:, 0]] * npp[tv[:, 1]]).sum()
+        self._prim_quartets = None
         self.stats["quartets_fp64"] = nq64
         self.stats["quartets_fp32"] = nq32
         self.stats["quartets"] = nq64 + nq32

@@ -216,11 +216,26 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                 torch.cuda.synchronize()
                 g = torch.cuda.CUDAGraph()
                 c0 = _lib_launches()
-                with torch.cuda.graph(g):
-                    fock_and_diis(True)
-                    diag_refine()
-                    density()
+                # captured on a side stream with the graph pool, without the
+                # torch.cuda.graph context's gc.collect() and empty_cache() (which
+                # would hand the allocator's cached blocks back to the driver)
+                side, pool = _graph_stream_and_pool(dev)
+                side.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(side):
+                    g.capture_begin(pool=pool)
+                    try:
+                        fock_and_diis(True)
+                        diag_refine()
+                        density()
+                    finally:
+                        g.capture_end()
+                torch.cuda.current_stream().wait_stream(side)
+                # keeps the pool alive (its use count) until the next solve's capture;
+                # the graph it replaces returns its blocks to the pool
+                _LAST_GRAPH[dev] = g
                 per_replay = _lib_launches() - c0
+                if record:
+                    phases["capture"] = time.perf_counter()
             g.replay()
             _lib_add_launches(per_replay)
         host = vals.cpu().numpy()
@@ -241,7 +256,7 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
                 # where it stopped, then the Jacobi route
                 fallbacks += 1
                 for _ in range(4):
-                    _, V, chk = eigen.refine_projector(Fx, Q, nocc, steps=2, check=True)
+                    _, V, chk = eigen.refine_projector(Fx, Q, nocc, steps=3, check=True, ortho_steps=2)
                     Q.copy_(V)
                     c = chk.cpu().numpy()
                     if c[0] <= 1e-10 and c[1] <= ov_tol and c[2] < 0.0:
@@ -285,6 +300,21 @@ def rhf(engine, max_iter=128, e_tol=1e-10, d_tol=1e-8, diis_size=10, diis_start=
         phases["final"] = time.perf_counter()
     return SCFResult(phases=phases, E=E, E_elec=E - e_nuc, E_nuc=e_nuc, C=Cf, eps=eps, D=Dn, F=F, iterations=it,
                      converged=converged, history=history, fock_builds=it, diag_fallbacks=fallbacks)
+
+
+_GRAPH_POOLS = {}
+_LAST_GRAPH = {}
+
+
+def _graph_stream_and_pool(dev):
+    """A capture stream and one memory pool per device for the SCF iteration graphs:
+    a new solve's capture takes its buffers from the pool, where the graph before the
+    previous one left them (the previous graph is kept, never replayed again, until
+    the capture that replaces it, so that the pool stays in use)."""
+    if dev not in _GRAPH_POOLS:
+        with torch.cuda.device(dev):
+            _GRAPH_POOLS[dev] = (torch.cuda.Stream(), torch.cuda.graph_pool_handle())
+    return _GRAPH_POOLS[dev]
 
 
 def _lib_launches():
