@@ -262,79 +262,6 @@ def exact_eigh_many(As, X_prevs=None, steps=4):
     return [_sort(torch.cat(wl), torch.cat(vl, dim=1)) for wl, vl in parts]
 
 
-def purify(A, nocc, max_iter=120, tol=1e-12):
-    """Projector onto the eigenvectors of the nocc lowest eigenvalues of symmetric A,
-    by canonical purification (A. H. R. Palser and D. E. Manolopoulos, Phys. Rev. B 58
-    (1998) 12704): P0 = lam/n (mu I - A) + nocc/n I with mu = tr(A)/n and lam from
-    Gershgorin bounds of the spectrum, then, with c = tr(P^2 - P^3) / tr(P - P^2),
-    P <- ((1 + c) P^2 - P^3) / c for c >= 1/2, else ((1 - 2c) P + (1 + c) P^2 - P^3) /
-    (1 - c).  The trace stays nocc and P converges to idempotency (quadratically at
-    the end); the step coefficients are formed on the device and the host reads the
-    idempotency error every fourth step.  FP64, library GEMMs."""
-    n = A.shape[0]
-    dev = A.device
-    I = torch.eye(n, dtype=torch.float64, device=dev)
-    d = torch.diagonal(A)
-    r = A.abs().sum(dim=1) - d.abs()
-    emin, emax = torch.min(d - r), torch.max(d + r)
-    mu = torch.trace(A) / n
-    lam = torch.minimum(nocc / (emax - mu), (n - nocc) / (mu - emin))
-    P = (lam / n) * (mu * I - A) + (nocc / n) * I
-    P2 = torch.empty_like(P)
-    P3 = torch.empty_like(P)
-    for it in range(max_iter):
-        dense.mm(P, P, out=P2)
-        dense.mm(P2, P, out=P3)
-        t1, t2, t3 = torch.trace(P), torch.trace(P2), torch.trace(P3)
-        den = t1 - t2
-        c = torch.where(den.abs() > 1e-300, (t2 - t3) / torch.where(den.abs() > 1e-300, den, 1.0), 0.5)
-        ge = c >= 0.5
-        ca = torch.where(ge, 0.0, (1.0 - 2.0 * c) / (1.0 - c))
-        cb = torch.where(ge, (1.0 + c) / c, (1.0 + c) / (1.0 - c))
-        cg = torch.where(ge, -1.0 / c, -1.0 / (1.0 - c))
-        P = ca * P + cb * P2 + cg * P3
-        if it % 4 == 3 and float(den) < tol * n:
-            break
-    return 0.5 * (P + P.T)
-
-
-def rotate_blocks(A, V, cuts, tol=1e-4, max_sweeps=5):
-    """V with each column block [cuts[k], cuts[k+1]) rotated to the FP32 Jacobi
-    eigenvectors of its projected block V_k^T A V_k, every block in one batched
-    launch; the blocks' spans are unchanged and each block of X^T A X becomes
-    nearly diagonal, which projector refinement needs to converge quadratically."""
-    blks = [V[:, a:b] for a, b in zip(cuts[:-1], cuts[1:])]
-    mats = []
-    for blk in blks:
-        Ab = dense.mm(blk, dense.mm(A, blk), ta=True)
-        mats.append(0.5 * (Ab + Ab.T))
-    m = max(a.shape[0] for a in mats)
-    m += m & 1
-    w, U = _jacobi(_padded(mats, m), True, max_sweeps, tol)
-    w, U = _sort(w, U.to(torch.float64))
-    return torch.cat([dense.mm(blk, U[k, :a.shape[0], :a.shape[0]].contiguous())
-                      for k, (blk, a) in enumerate(zip(blks, mats))], dim=1)
-
-
-def projector_basis(P, nocc, seed=0):
-    """An orthonormal basis (n x n) whose first nocc columns span the range of the
-    projector P and the rest its complement: each block from a seeded Gaussian matrix
-    projected (P G, (I - P) G), orthonormalised by Y (Y^T Y)^-1/2 (coupled
-    Newton-Schulz), projected and orthonormalised once more."""
-    n = P.shape[0]
-    g = torch.Generator(device=P.device).manual_seed(seed)
-    G = torch.randn(n, n, dtype=torch.float64, device=P.device, generator=g)
-    out = []
-    for Y, occ in ((G[:, :nocc], True), (G[:, nocc:], False)):
-        for _ in range(2):
-            PY = dense.mm(P, Y)
-            Y = PY if occ else Y - PY
-            Z, _ = dense.inv_sqrt(dense.mm(Y, Y, ta=True))
-            Y = dense.mm(Y, Z)
-        out.append(Y)
-    return torch.cat(out, dim=1).contiguous()
-
-
 def eigh(A, X_prev=None, refine_steps=2, exact=True, check_tol=1e-10, nocc=None):
     """Ascending eigenvalues and eigenvectors of symmetric FP64 A (..., n, n).
 
