@@ -225,6 +225,7 @@ class GpuEngine:
         p["pf8"] = torch.empty(idx.numel() * 8, dtype=torch.float32, device=self.dev)
         # pair kinds ordered by (pair class, kept primitive pairs)
         npp = cnt.cpu().numpy().astype(np.int64)
+        self.h_npp = npp
         pc = pair_class(self.h_pairs["lA"], self.h_pairs["lB"]).astype(np.int64)
         mb = int(npp.max()) + 1
         uniq, inv = np.unique(pc * mb + npp, return_inverse=True)
@@ -260,22 +261,54 @@ class GpuEngine:
     # Methods/properties.py:20-23); schwarz(), build_tasks() and compute_eris() follow it
     scattering = None
 
-    def _eri(self, cls, tasks, ntask, store, fp32):
+    def _eri(self, cls, tasks, ntask, store, fp32, pairs=None):
+        pairs = self.pairs_t if pairs is None else pairs
         if self.scattering is not None:
             if fp32:
                 raise ValueError("scattering integrals are FP64 only")
-            _lib.call("pcg_scattering_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t),
+            _lib.call("pcg_scattering_class", cls, ctypes.byref(self.basis_t), ctypes.byref(pairs),
                       _ptr(tasks), ntask, float(self.scattering), _ptr(store), _stream())
             return
-        _lib.call("pcg_eri_class", cls, ctypes.byref(self.basis_t), ctypes.byref(self.pairs_t), _ptr(tasks), ntask,
+        _lib.call("pcg_eri_class", cls, ctypes.byref(self.basis_t), ctypes.byref(pairs), _ptr(tasks), ntask,
                   _ptr(store), 1 if fp32 else 0, _stream())
 
+    # bra primitive pairs per task in the Schwarz pass
+    schwarz_slice = 4
+
+    def _sliced_pairs(self, ids, nslice):
+        """A pair table of len(ids) * nslice bra slices -- slice s of pair k covers its
+        kept primitive pairs [s * schwarz_slice, (s + 1) * schwarz_slice) -- followed by
+        the len(ids) whole pairs, sharing the primitive arrays (device tensors kept in
+        the returned tuple)."""
+        p, ch = self.pd, self.schwarz_slice
+        idt = torch.as_tensor(ids, dtype=torch.int64).to(self.dev)
+        sl = torch.arange(nslice, dtype=torch.int64, device=self.dev)
+        rep = lambda x: torch.cat([x.repeat_interleave(nslice, dim=0), x])
+        off, cnt = p["ppoff"][idt].to(torch.int64), p["npp"][idt].to(torch.int64)
+        s_off = (off[:, None] + sl[None, :] * ch).reshape(-1)
+        s_cnt = (cnt[:, None] - sl[None, :] * ch).clamp(0, ch).reshape(-1)
+        keep = dict(A=rep(p["A"][idt]).contiguous(), B=rep(p["B"][idt]).contiguous(),
+                    AB=rep(p["AB"].view(-1, 3)[idt]).reshape(-1).contiguous(),
+                    ppoff=torch.cat([s_off, off]).to(torch.int32), npp=torch.cat([s_cnt, cnt]).to(torch.int32))
+        t = PairsT()
+        ctypes.memmove(ctypes.addressof(t), ctypes.addressof(self.pairs_t), ctypes.sizeof(PairsT))
+        t.npair = len(ids) * (nslice + 1)
+        for k, f in (("A", "A"), ("B", "B"), ("ppoff", "ppoff"), ("npp", "npp_of"), ("AB", "AB")):
+            setattr(t, f, keep[k].data_ptr())
+        t.ao4 = None
+        return t, keep
+
     def schwarz(self):
-        """Q[pair] = sqrt(max (mn|mn)) over the diagonal quartets (ab|ab)."""
+        """Q[pair] = sqrt(max (mn|mn)) over the diagonal quartets (ab|ab).  A diagonal
+        quartet of many primitive pairs (the oxygen 1s pair: 36, so 1,296 primitive
+        quartets) would run long on one thread, so the bra's kept primitive pairs are
+        split into slices of schwarz_slice, each slice one task against the whole ket
+        pair; the slices' integrals (linear in the primitive sum) are added in a fixed
+        order before the maximum."""
         Q = torch.zeros(self.npair, dtype=torch.float64, device=self.dev)
         pc = pair_class(self.h_pairs["lA"], self.h_pairs["lB"])
         self.diag_blocks = {}
-        npp = self.h_pairs["npp"]
+        npp = self.h_npp
         for c in np.unique(pc):
             ids = np.nonzero(pc == c)[0].astype(np.int32)
             # heaviest pairs first: the warps run uniform primitive loops and the long
@@ -283,11 +316,23 @@ class GpuEngine:
             ids = ids[np.argsort(-npp[ids], kind="stable")]
             la, lb = int(self.h_pairs["lA"][ids[0]]), int(self.h_pairs["lB"][ids[0]])
             cls = _lib.load().pcg_eri_class_id(la, lb, la, lb)
-            tasks = self._t(np.stack([ids, ids], axis=1))
+            m = len(ids)
             nout = _lib.load().pcg_eri_class_nout(cls)
-            store = torch.empty(nout * len(ids), dtype=torch.float64, device=self.dev)
-            self._eri(cls, tasks, len(ids), store, False)
-            _lib.call("pcg_schwarz_class", cls, _ptr(tasks), len(ids), _ptr(store), _ptr(Q), _stream())
+            nslice = 1 if self.scattering is not None else max(1, -(-int(npp[ids].max()) // self.schwarz_slice))
+            if nslice == 1:
+                tasks = self._t(np.stack([ids, ids], axis=1))
+                store = torch.empty(nout * m, dtype=torch.float64, device=self.dev)
+                self._eri(cls, tasks, m, store, False)
+            else:
+                pairs, keep = self._sliced_pairs(ids, nslice)
+                vt = np.stack([np.arange(m * nslice), m * nslice + np.repeat(np.arange(m), nslice)], axis=1)
+                vtasks = self._t(vt.astype(np.int32))
+                part = torch.empty(nout * m * nslice, dtype=torch.float64, device=self.dev)
+                self._eri(cls, vtasks, m * nslice, part, False, pairs=pairs)
+                store = part.view(nout, m, nslice).sum(dim=2).contiguous()
+                tasks = self._t(np.stack([ids, ids], axis=1))
+                del keep
+            _lib.call("pcg_schwarz_class", cls, _ptr(tasks), m, _ptr(store), _ptr(Q), _stream())
         self.Q = Q
         return Q
 
