@@ -73,3 +73,24 @@ def test_noalloc_fock_rejects_bad_layout_before_any_cuda_call(lib):
                                       ctypes.cast(ptrs, ctypes.c_void_p), ctypes.cast(ntask, ctypes.c_void_p),
                                       ctypes.cast(ptrs, ctypes.c_void_p), fake, fake, fake, None) == 2
     assert b"bad class entry 1" in lib.pcg_last_error()
+
+
+def test_mp2_entry_points_reject_bad_arguments_before_any_cuda_call(lib):
+    # the compact-pair and pair-sum entry points of the MP2 path check their
+    # arguments first, so these refused calls need no GPU
+    import ctypes
+    from pychem_gb300._lib import BasisT, PairsT
+    fake = ctypes.c_void_p(16)          # never dereferenced: every call below is rejected
+    assert lib.pcg_mp2_pair_sums(0, 4, fake, fake, fake, fake, None) == 2
+    assert b"pcg_mp2_pair_sums" in lib.pcg_last_error()
+    assert lib.pcg_mp2_pair_sums(4, 4, None, fake, fake, fake, None) == 2
+    assert lib.pcg_mark_pairs(fake, 10, None, None) == 2
+    assert lib.pcg_mark_pairs(None, 10, fake, None) == 2
+    assert lib.pcg_pair_colmap(0, None, fake, None) == 2
+    assert lib.pcg_pair_colmap(8, None, None, None) == 2
+    assert lib.pcg_unpack_pairs(4, 8, 36, None, fake, fake, None) == 2
+    assert b"pcg_unpack_pairs" in lib.pcg_last_error()
+    b, p = BasisT(), PairsT()
+    assert lib.pcg_sym_pairs_class(0, ctypes.byref(b), ctypes.byref(p), fake, 1, fake, None, 10, fake, None) == 2
+    assert lib.pcg_sym_pairs_class(0, ctypes.byref(b), ctypes.byref(p), fake, 1, fake, fake, 0, fake, None) == 2
+    assert lib.pcg_sym_pairs_class(21, ctypes.byref(b), ctypes.byref(p), fake, 1, fake, fake, 10, fake, None) == 2
