@@ -30,27 +30,48 @@ __global__ void __launch_bounds__(DG_T* DG_T)
     k_dgemm(int M, int N, int K, double alpha, const double* __restrict__ A, long long sAb, long long sAm,
             long long sAk, const double* __restrict__ B, long long sBb, long long sBk, long long sBn, double beta,
             double* __restrict__ C, long long sCb, long long sCm, long long sCn) {
-  __shared__ double As[DG_T][DG_K + 1], Bs[DG_K][DG_T + 1];
+  // two shared-memory stages: the next K step's tile is loaded into registers while
+  // the current one is multiplied, so the global-load latency overlaps the FMAs
+  __shared__ double As[2][DG_T][DG_K + 1], Bs[2][DG_K][DG_T + 1];
+  constexpr int PER = DG_T * DG_K / (DG_T * DG_T);   // elements of each tile per thread
   const int tid = threadIdx.x, tx = tid % DG_T, ty = tid / DG_T;
   const long long b = blockIdx.z;
   const int m0 = blockIdx.y * DG_T, n0 = blockIdx.x * DG_T;
   const int m = m0 + ty, n = n0 + tx;
   A += b * sAb;
   B += b * sBb;
-  double acc = 0.0;
-  for (int k0 = 0; k0 < K; k0 += DG_K) {
+  double ra[PER], rb[PER];
+  auto load = [&](int k0) {
 #pragma unroll
-    for (int e = tid; e < DG_T * DG_K; e += DG_T * DG_T) {
-      const int r = e / DG_K, kk = e % DG_K;
-      const int mr = m0 + r, ka = k0 + kk;
-      As[r][kk] = (mr < M && ka < K) ? __ldg(A + mr * sAm + ka * sAk) : 0.0;
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + u * DG_T * DG_T;
+      const int mr = m0 + e / DG_K, ka = k0 + e % DG_K;
+      ra[u] = (mr < M && ka < K) ? __ldg(A + mr * sAm + ka * sAk) : 0.0;
       const int kb = k0 + e / DG_T, c = n0 + e % DG_T;
-      Bs[e / DG_T][e % DG_T] = (kb < K && c < N) ? __ldg(B + kb * sBk + c * sBn) : 0.0;
+      rb[u] = (kb < K && c < N) ? __ldg(B + kb * sBk + c * sBn) : 0.0;
     }
-    __syncthreads();
+  };
+  auto store = [&](int st) {
 #pragma unroll
-    for (int kk = 0; kk < DG_K; ++kk) acc = fma(As[ty][kk], Bs[kk][tx], acc);
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + u * DG_T * DG_T;
+      As[st][e / DG_K][e % DG_K] = ra[u];
+      Bs[st][e / DG_T][e % DG_T] = rb[u];
+    }
+  };
+  double acc = 0.0;
+  load(0);
+  store(0);
+  __syncthreads();
+  int st = 0;
+  for (int k0 = 0; k0 < K; k0 += DG_K) {
+    const bool more = k0 + DG_K < K;
+    if (more) load(k0 + DG_K);
+#pragma unroll
+    for (int kk = 0; kk < DG_K; ++kk) acc = fma(As[st][ty][kk], Bs[st][kk][tx], acc);
+    if (more) store(st ^ 1);
     __syncthreads();
+    st ^= 1;
   }
   if (m < M && n < N) {
     double* c = C + b * sCb + m * sCm + n * sCn;

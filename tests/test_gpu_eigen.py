@@ -84,3 +84,25 @@ def test_fp32_eigh_with_previous_vectors(n):
     assert (w2 - ref2).abs().max().item() < 2e-5 * scale * n ** 0.5
     resid = A2.float() @ V2 - V2 * w2.float().unsqueeze(-2)
     assert resid.abs().max().item() < 1e-4 * scale * n ** 0.5
+
+
+@pytest.mark.parametrize("M,N,K", [(1, 1, 1), (7, 13, 5), (208, 208, 208), (208, 80, 208), (33, 65, 97),
+                                   (298, 298, 298), (64, 1, 300)])
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+def test_dgemm_against_torch(M, N, K, ta, tb):
+    """pcg_dgemm (double-buffered 8 x 8 tiles, K steps of 32) against torch's FP64 matmul,
+    with transposes through strides, alpha/beta, and a batch of 3."""
+    from pychem_gb300 import dense
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N * 3 + K)
+    A = torch.randn(3, K, M, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(3, N, K, dtype=torch.float64, device="cuda", generator=g)
+    A = A.transpose(-1, -2) if not ta else A           # op(A) is M x K either way
+    A = A if not ta else A.contiguous()
+    B = B.transpose(-1, -2) if not tb else B
+    opA = A.transpose(-1, -2) if ta else A
+    opB = B.transpose(-1, -2) if tb else B
+    C0 = torch.randn(3, M, N, dtype=torch.float64, device="cuda", generator=g)
+    out = C0.clone()
+    dense.mm(A, B, ta=ta, tb=tb, out=out, alpha=0.5, beta=-2.0)
+    ref = 0.5 * (opA @ opB) - 2.0 * C0
+    assert (out - ref).abs().max().item() < 1e-12 * max(1.0, K ** 0.5)
