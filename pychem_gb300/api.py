@@ -16,11 +16,16 @@ def rhf_mp2(coords, basis="6-31G", charge=0, multiplicity=1, units="ANGSTROM", p
             fp32_below=1e-4, mp2=True, device="cuda", e_tol=1e-10, d_tol=1e-8):
     mol = Molecule(coords, basis, charge=charge, multiplicity=multiplicity, units=units)
     eng = GpuEngine(mol, device=device, precision=precision, fp32_below=fp32_below).prepare()
+    # MP2's pair tensor needs only the ERI store: it is built beside the SCF
+    pre = eng.prefetch_mp2_tensor() if mp2 else None
     res = rhf(eng, e_tol=e_tol, d_tol=d_tol)
     out = dict(E_rhf=res.E, E_nuc=res.E_nuc, iterations=res.iterations, converged=res.converged,
                nbf=mol.NOrbitals, quartets=eng.stats["quartets"])
     if mp2:
-        e2 = rmp2(eng, res.C, res.eps)
+        eri, ready = pre
+        torch.cuda.current_stream().wait_event(ready)
+        e2 = rmp2(eng, res.C, res.eps, eri=eri)
+        del eri
         out["E_mp2_corr"] = e2
         out["E_mp2_total"] = res.E + e2
     out["mo_energies"] = res.eps.cpu().numpy()

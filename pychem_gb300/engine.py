@@ -529,6 +529,24 @@ class GpuEngine:
         E = E.view(rows, n, n)
         return (E, pmap, rows) if compact else E
 
+    def prefetch_mp2_tensor(self):
+        """Start dense_eri_pairs(compact=True) on a side stream -- it reads only the ERI
+        store -- so that it runs beside the SCF (whose first iteration and final
+        orbitals leave most SMs idle).  Returns ((E, map, rows), event): the tuple is
+        for scf.rmp2(eri=...) once the current stream has waited for the event."""
+        main = torch.cuda.current_stream(self.dev)
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream(self.dev)
+        side = self._side
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            E, pmap, rows = self.dense_eri_pairs(compact=True)
+            ev = torch.cuda.Event()
+            ev.record(side)
+        E.record_stream(main)
+        pmap.record_stream(main)
+        return (E, pmap, rows), ev
+
     def dense_eri(self):
         """Dense nbf^4 tensor (8-fold symmetric fill), zero where screened out."""
         n = self.nbf
