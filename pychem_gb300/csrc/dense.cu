@@ -249,7 +249,7 @@ extern "C" int pcg_diis_step(long long len, int cap, int* state, const double* F
   cudaStream_t s = (cudaStream_t)stream;
   const unsigned blocks = (unsigned)((len + 255) / 256);
   k_diis_store<<<blocks, 256, 0, s>>>(len, cap, state, F, R, focks, resids);
-  k_diis_dots<<<cap, 256, 0, s>>>(len, cap, state, R, resids, row);
+  k_diis_dots<<<cap, 1024, 0, s>>>(len, cap, state, R, resids, row);
   k_diis_solve<<<1, 32, 0, s>>>(cap, state, row, Bm, coef);
   k_diis_extrapolate<<<blocks, 256, 0, s>>>(len, cap, coef, focks, Fx);
   PCG_CUDA(cudaGetLastError());

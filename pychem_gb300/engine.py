@@ -88,19 +88,26 @@ def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32, kind_work=None):
     hi = torch.searchsorted(seg_key, key, right=True)
     nbits = int((hi - lo).max()).bit_length() + 1 if pos.numel() else 0
 
-    def prefix(t):
-        # largest c in [0, hi - lo] with qb * Qs[lo + c - 1] > t (Qs descending in a segment)
-        a = torch.zeros_like(lo)
-        b = hi - lo
+    def prefix(ts):
+        # for each threshold t of ts: the largest c in [0, hi - lo] with
+        # qb * Qs[lo + c - 1] > t (Qs descending in a segment); both thresholds bisect
+        # together, one set of tensor operations per step
+        tt = torch.tensor(ts, dtype=Qs.dtype, device=dev)[:, None]
+        a = torch.zeros((len(ts), lo.numel()), dtype=lo.dtype, device=dev)
+        b = (hi - lo).expand(len(ts), -1).clone()
         for _ in range(nbits):
             mid = (a + b + 1) // 2
-            ok = (mid > 0) & (qb * Qs[(lo + mid - 1).clamp(0, max(npair - 1, 0))] > t)
+            ok = (mid > 0) & (qb * Qs[(lo + mid - 1).clamp(0, max(npair - 1, 0))] > tt)
             a = torch.where(ok, mid, a)
             b = torch.where(ok, b, mid - 1)
         return a
 
-    c = prefix(thr)
-    c32 = torch.minimum(prefix(thr32), c) if thr32 > 0 else c
+    if thr32 > 0:
+        c, c32 = prefix([thr, thr32])
+        c32 = torch.minimum(c32, c)
+    else:
+        c = prefix([thr])[0]
+        c32 = c
     same = kk == kb
     r = pos - lo
     cnt = torch.where(same, torch.minimum(r + 1, c), c)

@@ -44,12 +44,13 @@ def orthogonaliser(S, canonical=False):
     if not canonical and n > eigen.FP64_JACOBI_MAX_N:
         X, ok = dense.inv_sqrt(S)
         if ok:
+            # power iteration on X^2 = S^-1, on the device; the host reads the result once
             v = torch.ones(n, 1, dtype=S.dtype, device=S.device) / math.sqrt(n)
-            mu = 1.0
             for _ in range(16):
                 w = dense.mm(X, dense.mm(X, v))
-                mu = float(torch.linalg.vector_norm(w))
-                v = w / mu
+                nrm = torch.linalg.vector_norm(w)
+                v = w / nrm
+            mu = float(nrm)
             if 1.0 / mu > 10.0 * LINEAR_DEPENDENCE:
                 return X
     s, U = eigen.eigh(S, exact=True)
