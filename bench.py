@@ -771,7 +771,12 @@ def gpu_arm(args):
                      "achieved": tc_flops / tc_t / 1e12, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
                      "frac": (tc_flops / tc_t / 1e12) / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
-                     "traffic": None, "algorithmic_flops_per_launch": tc_flops / max(1, len(tl)),
+                     "traffic": tc_bytes / max(1, len(tl)),
+                     "traffic_source": "ncu capture of one launch at the first transform's shape "
+                                       "(profiles/ozaki_tc_gemm_mp2_shape.md): DRAM reads = the FP64 input "
+                                       "once, writes = the FP64 output; scaled to each launch's M, N, K and "
+                                       "averaged per launch",
+                     "algorithmic_flops_per_launch": tc_flops / max(1, len(tl)),
                      "launches": len(tl), "seconds": tc_t,
                      "fp64_operand_and_output_bytes": tc_bytes},
         "roofline_eri": {"bound": "fp64", "kernel": "ERI class kernels k_eri<*> (FP64 pipe)",
