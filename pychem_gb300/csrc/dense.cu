@@ -263,29 +263,38 @@ extern "C" int pcg_diis_step(long long len, int cap, int* state, const double* F
 //   s1 = sum X(i,a,j,b)^2 / D,  s2 = sum X(i,a,j,b) X(i,b,j,a) / D,
 //   D = e_i + e_j - e_a - e_b.
 // Both summands are symmetric under (i,a) <-> (j,b); block p = b*o + j takes the
-// pairs q = a*o + i <= p, weight 2 below the diagonal.  1/D: the FP32 reciprocal and
-// one Newton step in FP64 (relative error ~ 2^-46).  part[2p], part[2p+1]: the block's
+// pairs q = a*o + i <= p, weight 2 below the diagonal.  1/D: the FP32 reciprocal of
+// the denominator formed from FP32 copies of the energies, then one Newton step
+// against the FP64 denominator (relative error ~ 1e-13).  part[2p], part[2p+1]: the block's
 // s1 and s2 (summed on the host side of the call, in a fixed order).
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_mp2_pair_sums(int o, int v, const double* __restrict__ X,
                                                        const double* __restrict__ eo, const double* __restrict__ ev,
                                                        double* __restrict__ part) {
-  extern __shared__ double e_sh[];                 // eo (o), then ev (v)
-  for (int t = threadIdx.x; t < o + v; t += blockDim.x) e_sh[t] = t < o ? eo[t] : ev[t - o];
+  extern __shared__ double e_sh[];                 // eo (o), then ev (v); then their FP32 copies
+  float* ef = (float*)(e_sh + o + v);
+  for (int t = threadIdx.x; t < o + v; t += blockDim.x) {
+    const double e = t < o ? eo[t] : ev[t - o];
+    e_sh[t] = e;
+    ef[t] = (float)e;
+  }
   __syncthreads();
   const int p = blockIdx.x, b = p / o, j = p % o;
   const double ejb = e_sh[j] - e_sh[o + b];
+  const float fjb = ef[j] - ef[o + b];
   const double* Xp = X + (size_t)p * v * o;                       // X(., ., j, b)
   const int step = blockDim.x, da = step / o, di = step % o;
   int a = threadIdx.x / o, i = threadIdx.x % o;
   double s1 = 0.0, s2 = 0.0;
+  // every pair q <= p with weight 1; the block total is 2 * sum - (the q = p term)
   for (int q = threadIdx.x; q <= p; q += step) {
     const double x = Xp[q];
     const double xe = X[((size_t)(a * o + j) * v + b) * o + i];   // X(i, b, j, a)
     const double d = (e_sh[i] - e_sh[o + a]) + ejb;
-    double r = (double)__frcp_rn((float)d);
+    // FP32 seed from the FP32 energies, one Newton step against the FP64 denominator
+    double r = (double)__frcp_rn((ef[i] - ef[o + a]) + fjb);
     r = fma(r, fma(-d, r, 1.0), r);
-    const double t = (q < p ? 2.0 : 1.0) * x * r;
+    const double t = x * r;
     s1 = fma(x, t, s1);
     s2 = fma(xe, t, s2);
     i += di; a += da;
@@ -302,19 +311,21 @@ __global__ void __launch_bounds__(256) k_mp2_pair_sums(int o, int v, const doubl
   if (threadIdx.x == 0) {
     double r1 = 0.0, r2 = 0.0;
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { r1 += red[0][k]; r2 += red[1][k]; }
-    part[2 * (size_t)p] = r1;
-    part[2 * (size_t)p + 1] = r2;
+    const double xd = Xp[p];                       // (jb|jb), its own exchange partner
+    const double dg = xd * xd / (2.0 * ejb);
+    part[2 * (size_t)p] = 2.0 * r1 - dg;
+    part[2 * (size_t)p + 1] = 2.0 * r2 - dg;
   }
 }
 
 extern "C" int pcg_mp2_pair_sums(int o, int v, const double* X, const double* eo, const double* ev, double* part,
                                  void* stream) {
   if (o < 1 || v < 1 || !X || !eo || !ev || !part || (long long)o * v > 0x7fffffffLL ||
-      (size_t)(o + v) * sizeof(double) > 200 * 1024) {
+      (size_t)(o + v) * (sizeof(double) + sizeof(float)) > 200 * 1024) {
     pcg_set_error("pcg_mp2_pair_sums: bad arguments");
     return PCG_ERR_ARG;
   }
-  const size_t sh = (size_t)(o + v) * sizeof(double);
+  const size_t sh = (size_t)(o + v) * (sizeof(double) + sizeof(float));
   if (sh > 48 * 1024) PCG_CUDA(cudaFuncSetAttribute(k_mp2_pair_sums, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
   k_mp2_pair_sums<<<o * v, 256, sh, (cudaStream_t)stream>>>(o, v, X, eo, ev, part);
   PCG_CUDA(cudaGetLastError());

@@ -249,9 +249,20 @@ __global__ void __launch_bounds__(512) k_unpack_rows(long long R, int nn, int le
       __syncthreads();
     }
     double* dst = out + r * nn;
-    for (int ab = threadIdx.x; ab < nn; ab += blockDim.x) {
-      const int q = __ldg(colmap + ab);
-      __stcs(dst + ab, q < 0 ? 0.0 : (SH ? row_sh[q] : __ldg(src + q)));
+    if (SH && (nn & 1) == 0) {
+      // two elements per thread: one 8-byte map load and one 16-byte store (rows of an
+      // even length keep the output 16-byte aligned)
+      const int2* cm2 = (const int2*)colmap;
+      double2* d2 = (double2*)dst;
+      for (int h = threadIdx.x; h < nn / 2; h += blockDim.x) {
+        const int2 q = __ldg(cm2 + h);
+        __stcs(d2 + h, make_double2(q.x < 0 ? 0.0 : row_sh[q.x], q.y < 0 ? 0.0 : row_sh[q.y]));
+      }
+    } else {
+      for (int ab = threadIdx.x; ab < nn; ab += blockDim.x) {
+        const int q = __ldg(colmap + ab);
+        __stcs(dst + ab, q < 0 ? 0.0 : (SH ? row_sh[q] : __ldg(src + q)));
+      }
     }
   }
 }
