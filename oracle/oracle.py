@@ -16,7 +16,7 @@ import this module, always as the checker.  It restates the upstream algorithm:
   residual X^T(SDF - FDS)X (``Methods/hf_extensions/diis.py:14-139``), energy
   0.5 sum(D_tot H + D_a F_a + D_b F_b) (``Methods/hartree_fock.py:188-201``).
   ``mode='reference'`` keeps upstream's choices (energy from the extrapolated Fock,
-  |dE| stop only); ``mode='consistent'`` (the default judge) takes the energy from the
+  |dE| stop only); ``mode='consistent'`` (the default checker) takes the energy from the
   Fock built from the current density and stops on |dE| < 1e-10 and D-RMS < 1e-8.
 * MP2: closed-shell form of ``Methods/mp2.py:43-94`` (identical value for RHF).
 * Open shells: UHF and CUHF along ``Methods/hartree_fock.py:23-142`` with the per-spin

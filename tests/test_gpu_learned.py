@@ -1,5 +1,5 @@
 """Learned initial guess: forward/backward kernels against the FP64 CPU oracle, and the
-trained network's effect on the SCF (the SAD-guess SCF stays the judge)."""
+trained network's effect on the SCF (the SAD-guess SCF stays the reference result)."""
 import os
 
 import numpy as np
