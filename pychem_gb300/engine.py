@@ -116,12 +116,21 @@ def plan_quartets(Q, kind, mol, nmol, class_table, thr, thr32, kind_work=None):
     cls_row = class_table[kb, kk]
     bra = o[pos]
     plan = []
+    ncls = int(class_table.max()) + 1 if class_table.numel() else 0
     for part, n, qs, dg in (("64", c64 + diag, lo, diag), ("32", cnt - c64, lo + c64, torch.zeros_like(diag))):
-        live = n > 0
-        for cls in torch.unique(cls_row[live]).tolist():
-            sel = ((cls_row == cls) & live).nonzero().squeeze(1)
+        # rows grouped by class (a stable sort keeps each class's rows in order), the
+        # class sizes read back once per part
+        key = torch.where(n > 0, cls_row, torch.full_like(cls_row, ncls))
+        order = torch.sort(key, stable=True).indices
+        counts = torch.bincount(key, minlength=ncls + 1)[:ncls].tolist()
+        start = 0
+        for cls, c in enumerate(counts):
+            if c == 0:
+                continue
+            sel = order[start:start + c]
+            start += c
             off = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), torch.cumsum(n[sel], 0)])
-            plan.append((int(cls), part, bra[sel], off, qs[sel], dg[sel]))
+            plan.append((cls, part, bra[sel], off, qs[sel], dg[sel]))
     return plan, o
 
 
