@@ -94,3 +94,25 @@ def test_mp2_entry_points_reject_bad_arguments_before_any_cuda_call(lib):
     assert lib.pcg_sym_pairs_class(0, ctypes.byref(b), ctypes.byref(p), fake, 1, fake, None, 10, fake, None) == 2
     assert lib.pcg_sym_pairs_class(0, ctypes.byref(b), ctypes.byref(p), fake, 1, fake, fake, 0, fake, None) == 2
     assert lib.pcg_sym_pairs_class(21, ctypes.byref(b), ctypes.byref(p), fake, 1, fake, fake, 10, fake, None) == 2
+
+
+def _declared_arities():
+    """name -> number of parameters of every pcg_* prototype in include/*.h."""
+    out = {}
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"\b(pcg_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+            params = m.group(2).strip()
+            out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_binding_arities_match_the_prototypes():
+    # the ctypes argument lists of pychem_gb300/_lib.py have as many entries as the
+    # header's prototypes have parameters (a drift here would pass wrong arguments)
+    from pychem_gb300 import _lib
+    ar = _declared_arities()
+    assert len(ar) >= 25
+    bad = {n: (ar[n], len(_lib._SIGS[n])) for n in ar if n in _lib._SIGS and ar[n] != len(_lib._SIGS[n])}
+    assert not bad, bad
