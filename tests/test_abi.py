@@ -116,3 +116,31 @@ def test_binding_arities_match_the_prototypes():
     assert len(ar) >= 25
     bad = {n: (ar[n], len(_lib._SIGS[n])) for n in ar if n in _lib._SIGS and ar[n] != len(_lib._SIGS[n])}
     assert not bad, bad
+
+
+def test_binding_types_match_the_prototypes():
+    # each ctypes argument type matches the C parameter type: pointers as pointers,
+    # and int / long long / size_t / double / float by width (an int passed where the
+    # prototype has long long would leave the upper half undefined)
+    import ctypes
+    from pychem_gb300 import _lib
+    kinds = {"long long": ctypes.c_longlong, "size_t": ctypes.c_size_t, "double": ctypes.c_double,
+             "float": ctypes.c_float, "int": ctypes.c_int}
+    bad = []
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"\b(pcg_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+            name, params = m.group(1), m.group(2).strip()
+            if name not in _lib._SIGS or params in ("", "void"):
+                continue
+            for k, (p, t) in enumerate(zip(params.split(","), _lib._SIGS[name])):
+                p = " ".join(p.replace("const", " ").split())
+                if "*" in p:
+                    ok = t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "_type_") and t.__name__.startswith("LP_")
+                else:
+                    base = next((c for key, c in kinds.items() if p.startswith(key + " ") or p == key), None)
+                    ok = base is not None and ctypes.sizeof(base) == ctypes.sizeof(t) and \
+                        (base in (ctypes.c_double, ctypes.c_float)) == (t in (ctypes.c_double, ctypes.c_float))
+                if not ok:
+                    bad.append((name, k, p, t.__name__))
+    assert not bad, bad
